@@ -1,0 +1,169 @@
+/*
+ * isar_gb300.h -- plain C ABI of the GB300 ISAR imaging library
+ * (libisar_gb300.so).  Pointers and sizes only; no C++ or torch types.
+ *
+ * The library re-implements the single-image imaging chain of
+ * Junf137/isar_imaging_cuda (isarMainSingle -> ISAR_RD_Imaging_Main_Ku,
+ * isar_imaging/isar_main.cu:3-227) on hand-written sm_103a kernels.
+ * The reference's own seven exports (isar_imaging_export.h) are provided on
+ * top of this ABI, see isar_imaging_export.h in this directory.
+ *
+ * Data layout (as the reference): complex64 interleaved (re, im) float
+ * pairs, row-major [echo_num][range_num], row = pulse.  Images are float
+ * [echo_num][512], row = Doppler bin, column = range bin.
+ *
+ * Errors: every int-returning call returns ISAR_OK (0) or a negative
+ * ISAR_E* code; isar_get_last_error() gives the message of the calling
+ * thread's last failure.
+ */
+#ifndef ISAR_GB300_H_
+#define ISAR_GB300_H_
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#if defined(__GNUC__)
+#define ISAR_API __attribute__((visibility("default")))
+#else
+#define ISAR_API
+#endif
+
+enum {
+    ISAR_OK = 0,
+    ISAR_EINVAL = -1,   /* invalid argument or unsupported size            */
+    ISAR_ECUDA = -2,    /* CUDA runtime error                              */
+    ISAR_ENOMEM = -3,   /* device or host allocation failed                */
+    ISAR_ESTATE = -4,   /* call out of order (e.g. no frame imaged yet)    */
+    ISAR_EIO = -5       /* file I/O error (.wbd ingest)                    */
+};
+
+/* DATA_TYPE (isar_imaging/common.cuh:82-87) */
+enum { ISAR_DATA_IFDS = 1, ISAR_DATA_STRETCH = 2 };
+
+/* flags for one frame: if_hpc (isar_main.cu:33), if_mtrc (isar_main.cu:160) */
+enum { ISAR_FLAG_HPC = 1, ISAR_FLAG_MTRC = 2 };
+
+/* RadarParameters (isar_imaging/common.cuh:96-117) */
+typedef struct {
+    int echo_num;          /* M: pulses per image, power of two, 128..1024     */
+    int range_num;         /* N: range cells, power of two, 512..8192, >= M    */
+    long long band_width;  /* Hz                                               */
+    long long fc;          /* Hz                                               */
+    double Tp;             /* s                                                */
+    long long Fs;          /* Hz                                               */
+    int data_type;         /* ISAR_DATA_STRETCH or ISAR_DATA_IFDS              */
+} isar_radar;
+
+/* Decisions of the last imaged frame, for inspection and parity checks. */
+typedef struct {
+    float* ra_shift;          /* in: caller buffer of M-1 floats, or NULL    */
+    float* phase;             /* in: caller buffer of 2*M floats, or NULL    */
+    int center_applied;       /* HRRPCenter shifted the profiles             */
+    int center_shift;         /* shift_num, cells                            */
+    int cut_offset;           /* first range cell of the 512-cell cut        */
+    int center_idx1_len;
+    int center_idx2_len;
+    float center_threshold;
+    int tgt_num;              /* fastEntropy target range bins               */
+    int unit2_num;            /* U, bins used by the autofocus               */
+    int bins[512];            /* the U bins, ascending                       */
+} isar_trace;
+
+typedef struct isar_ctx isar_ctx;
+
+/* Copies the calling thread's last error message; returns its length. */
+ISAR_API int isar_get_last_error(char* buf, size_t len);
+
+/* Library version string. */
+ISAR_API const char* isar_version(void);
+
+/* Number of CUDA kernels this library has launched so far (all contexts). */
+ISAR_API long long isar_launch_count(void);
+
+/*
+ * Creates an imaging context on `device` for frames of radar->echo_num x
+ * radar->range_num: device workspace, twiddle/window/CZT tables and a
+ * stream (`stream` = an existing cudaStream_t to use, or NULL for a new one).
+ * Replaces imagingMemInit (isar_imaging_export.cpp:121-205).
+ */
+ISAR_API int isar_create(isar_ctx** out, const isar_radar* radar, int device, void* stream);
+ISAR_API int isar_destroy(isar_ctx* ctx);
+
+/* The stream the context launches on (cudaStream_t). */
+ISAR_API void* isar_stream(isar_ctx* ctx);
+
+/*
+ * One frame from host memory: echo = 2*M*N floats, velocity = M doubles
+ * (read only with ISAR_FLAG_HPC on STRETCH data, may be NULL otherwise),
+ * img = M*512 floats.  Blocking, like isarMainSingle
+ * (isar_imaging_export.cpp:208-212).
+ */
+ISAR_API int isar_image_host(isar_ctx* ctx, const float* echo, const double* velocity, int flags, float* img);
+
+/*
+ * One frame on device memory, stream-ordered on isar_stream(ctx), no host
+ * synchronisation.  d_echo (2*M*N floats) is only read; the range profiles
+ * (the reference's d_data_proc after range alignment) stay in the context,
+ * see isar_get_profiles.  d_velocity: M doubles on the device (or NULL
+ * without HPC).  d_img: M*512 floats.
+ */
+ISAR_API int isar_image_device(isar_ctx* ctx, const float* d_echo, const double* d_velocity, int flags, float* d_img);
+
+/* Device pointer of the context's M*N complex range profiles of the last
+ * frame (aligned, before centering). */
+ISAR_API int isar_get_profiles(isar_ctx* ctx, const float** d_profiles);
+
+/* Decisions of the last frame (synchronises the context stream). */
+ISAR_API int isar_get_trace(isar_ctx* ctx, isar_trace* out);
+
+/* ---- stage entry points (device pointers, stream-ordered, in place) ---- */
+
+/* highSpeedCompensation (high_speed_compensation.cu:4-54) applied to d_x. */
+ISAR_API int isar_stage_hpc(isar_ctx* ctx, float* d_x, const double* d_velocity);
+/* rangeAlignmentParallel (range_alignment.cu:4-78), with HPC fused in when
+ * flags has ISAR_FLAG_HPC: spectra in d_x -> complex range profiles. */
+ISAR_API int isar_stage_range_align(isar_ctx* ctx, float* d_x, const double* d_velocity, int flags);
+/* HRRPCenter (range_alignment.cu:371-465) + cutRangeProfile
+ * (common.cu:494-509): profiles d_y (M*N) -> d_cut (M*512). */
+ISAR_API int isar_stage_center_cut(isar_ctx* ctx, const float* d_y, float* d_cut);
+/* fastEntropy (phase_adjustment.cu:167-332) in place on d_cut. */
+ISAR_API int isar_stage_fast_entropy(isar_ctx* ctx, float* d_cut, int iterations);
+/* mtrc (mtrc.cu:4-76, when ISAR_FLAG_MTRC) and post-processing
+ * (isar_main.cu:191-211): d_cut -> d_img (M*512 floats). */
+ISAR_API int isar_stage_post(isar_ctx* ctx, float* d_cut, int flags, float* d_img);
+
+/* ---- synthetic dechirped echoes (benchmarks, training data) ------------ */
+typedef struct {
+    int M, N;                 /* pulses, range cells                              */
+    double fc, B, prf, Fs;    /* Hz                                               */
+    int n_scat;               /* point scatterers (Rayleigh amplitudes)           */
+    double patch_x, patch_y;  /* m: cross-range, range extent of the target patch */
+    double omega;             /* rad/s rotation rate                              */
+    double r0_cells;          /* range offset of the patch centre, cells          */
+    double drift_sigma;       /* cells: per-pulse random-walk range drift         */
+    double phase_uniform;     /* rad: half width of the uniform phase error       */
+    double phase_quad;        /* rad: quadratic phase error at the aperture edge  */
+    double v0, accel;         /* m/s, m/s^2: radial velocity (HPC term)           */
+    double snr_db;
+    double rms_counts;        /* ADC scale of the signal part (int16 counts)      */
+    uint64_t seed;
+} isar_synth_params;
+
+/* Writes one M x N frame of int16-quantised counts as complex64 into d_out
+ * (device), the quantised per-pulse velocities into d_velocity (device,
+ * may be NULL) and h_velocity (host, may be NULL).  Blocking on `stream`. */
+ISAR_API int isar_synth_device(const isar_synth_params* p, float* d_out, double* d_velocity, double* h_velocity,
+                               void* stream);
+
+/* Batched unnormalised row FFTs of length n (512..8192) in place, for tests. */
+ISAR_API int isar_fft_rows(isar_ctx* ctx, float* d_x, int rows, int n, int inverse);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* ISAR_GB300_H_ */

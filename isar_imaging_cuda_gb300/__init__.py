@@ -1,0 +1,253 @@
+"""GB300-native ISAR range-Doppler imaging (sm_103a).
+
+Python view of ``libisar_gb300.so`` through its plain C ABI
+(``include/isar_gb300.h``).  The library re-implements the imaging chain of
+Junf137/isar_imaging_cuda behind ``isarMainSingle``: high-speed compensation,
+range alignment, HRRP centering and cut, Doppler tracking + fast minimum
+entropy autofocus, CZT MTRC correction and image formation.
+
+Device buffers are passed as torch CUDA tensors (or raw integer device
+pointers).  The CUDA library must be built (``build.build()``); there is no
+CPU fallback: every call fails loudly when the extension is missing.
+"""
+import ctypes as C
+import os
+
+from . import build as _build
+
+STRETCH = 2
+IFDS = 1
+FLAG_HPC = 1
+FLAG_MTRC = 2
+RANGE_NUM_CUT = 512
+
+ISAR_OK = 0
+_ERRORS = {-1: "EINVAL", -2: "ECUDA", -3: "ENOMEM", -4: "ESTATE", -5: "EIO"}
+
+# every symbol the C headers declare with ISAR_API (checked by the tests)
+EXPORTS = ("isar_get_last_error", "isar_version", "isar_create", "isar_destroy", "isar_stream",
+           "isar_image_host", "isar_image_device", "isar_get_trace", "isar_stage_hpc",
+           "isar_stage_range_align", "isar_stage_center_cut", "isar_stage_fast_entropy",
+           "isar_stage_post", "isar_fft_rows", "isar_get_profiles", "isar_synth_device", "isar_launch_count")
+
+
+class IsarError(RuntimeError):
+    pass
+
+
+class Radar(C.Structure):
+    """isar_radar: RadarParameters (common.cuh:96-117) + data type."""
+    _fields_ = [("echo_num", C.c_int), ("range_num", C.c_int), ("band_width", C.c_longlong),
+                ("fc", C.c_longlong), ("Tp", C.c_double), ("Fs", C.c_longlong), ("data_type", C.c_int)]
+
+
+class SynthParams(C.Structure):
+    _fields_ = [("M", C.c_int), ("N", C.c_int), ("fc", C.c_double), ("B", C.c_double), ("prf", C.c_double),
+                ("Fs", C.c_double), ("n_scat", C.c_int), ("patch_x", C.c_double), ("patch_y", C.c_double),
+                ("omega", C.c_double), ("r0_cells", C.c_double), ("drift_sigma", C.c_double),
+                ("phase_uniform", C.c_double), ("phase_quad", C.c_double), ("v0", C.c_double),
+                ("accel", C.c_double), ("snr_db", C.c_double), ("rms_counts", C.c_double), ("seed", C.c_uint64)]
+
+
+class Trace(C.Structure):
+    _fields_ = [("ra_shift", C.c_void_p), ("phase", C.c_void_p), ("center_applied", C.c_int),
+                ("center_shift", C.c_int), ("cut_offset", C.c_int), ("center_idx1_len", C.c_int),
+                ("center_idx2_len", C.c_int), ("center_threshold", C.c_float), ("tgt_num", C.c_int),
+                ("unit2_num", C.c_int), ("bins", C.c_int * 512)]
+
+
+_lib = None
+
+
+def lib_path():
+    return _build.LIB
+
+
+def load(build_if_missing=True):
+    """Loads libisar_gb300.so (building it in-tree if missing)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    path = _build.LIB
+    if not os.path.exists(path):
+        if not build_if_missing:
+            raise IsarError("libisar_gb300.so is not built (run isar_imaging_cuda_gb300.build.build())")
+        _build.build()
+    lib = C.CDLL(path)
+    vp, i, d = C.c_void_p, C.c_int, C.c_double
+    sig = {
+        "isar_get_last_error": (i, [C.c_char_p, C.c_size_t]),
+        "isar_version": (C.c_char_p, []),
+        "isar_create": (i, [C.POINTER(vp), C.POINTER(Radar), i, vp]),
+        "isar_destroy": (i, [vp]),
+        "isar_stream": (vp, [vp]),
+        "isar_image_host": (i, [vp, vp, vp, i, vp]),
+        "isar_image_device": (i, [vp, vp, vp, i, vp]),
+        "isar_get_trace": (i, [vp, C.POINTER(Trace)]),
+        "isar_stage_hpc": (i, [vp, vp, vp]),
+        "isar_stage_range_align": (i, [vp, vp, vp, i]),
+        "isar_stage_center_cut": (i, [vp, vp, vp]),
+        "isar_stage_fast_entropy": (i, [vp, vp, i]),
+        "isar_stage_post": (i, [vp, vp, i, vp]),
+        "isar_fft_rows": (i, [vp, vp, i, i, i]),
+        "isar_get_profiles": (i, [vp, C.POINTER(vp)]),
+        "isar_synth_device": (i, [C.POINTER(SynthParams), vp, vp, vp, vp]),
+        "isar_launch_count": (C.c_longlong, []),
+    }
+    for name, (res, args) in sig.items():
+        f = getattr(lib, name)
+        f.restype = res
+        f.argtypes = args
+    _lib = lib
+    return lib
+
+
+def launch_count():
+    """Kernels launched by the library so far."""
+    return int(load().isar_launch_count())
+
+
+def last_error():
+    buf = C.create_string_buffer(1024)
+    load().isar_get_last_error(buf, len(buf))
+    return buf.value.decode(errors="replace")
+
+
+def _check(rc, what):
+    if rc != ISAR_OK:
+        raise IsarError("%s failed (%s): %s" % (what, _ERRORS.get(rc, rc), last_error()))
+
+
+def _dptr(t):
+    """Device pointer of a torch CUDA tensor (or an int)."""
+    if t is None:
+        return None
+    if isinstance(t, int):
+        return t
+    if not t.is_cuda:
+        raise IsarError("expected a CUDA tensor")
+    if not t.is_contiguous():
+        raise IsarError("expected a contiguous tensor")
+    return t.data_ptr()
+
+
+def radar(M, N, B=1.0e9, fc=10.0e9, Fs=100.0e6, Tp=None, data_type=STRETCH):
+    """Radar parameters of an M x N frame (Tp defaults to N / Fs)."""
+    if Tp is None:
+        Tp = N / Fs
+    return Radar(int(M), int(N), int(B), int(fc), float(Tp), int(Fs), int(data_type))
+
+
+def synth_params(M, N, seed, full=False, **kw):
+    """Seeded synthetic-frame parameters: the plain workload (50 scatterers in
+    20 m x 20 m, 0.02 rad/s, drift 0.3 cell, uniform phase error, SNR 10 dB,
+    no radial velocity) or, with full=True, the five-stage workload (200
+    scatterers in 40 m x 40 m, 4 degrees over the aperture, 3000 m/s and
+    50 m/s^2, drift 0.5 cell, quadratic + random phase error, SNR 5 dB)."""
+    import math
+    d = dict(fc=10e9, B=1e9, prf=1000.0, Fs=100e6, n_scat=50, patch_x=20.0, patch_y=20.0, omega=0.02,
+             r0_cells=20.0, drift_sigma=0.3, phase_uniform=math.pi, phase_quad=0.0, v0=0.0, accel=0.0,
+             snr_db=10.0, rms_counts=1000.0)
+    if full:
+        d.update(n_scat=200, patch_x=40.0, patch_y=40.0, omega=math.radians(4.0) / (M / 1000.0),
+                 drift_sigma=0.5, phase_uniform=0.5, phase_quad=6.0, v0=3000.0, accel=50.0, snr_db=5.0)
+    d.update(kw)
+    return SynthParams(M=M, N=N, seed=seed, **d)
+
+
+def synth_device(p: SynthParams, d_out, d_vel=None, stream=None):
+    """Generates one frame on the device; returns the host velocities (numpy)."""
+    import numpy as np
+    hv = np.zeros(p.M, np.float64)
+    _check(load().isar_synth_device(C.byref(p), _dptr(d_out), _dptr(d_vel), hv.ctypes.data,
+                                    C.c_void_p(stream) if stream else None), "isar_synth_device")
+    return hv
+
+
+class Context:
+    """An imaging context (workspace + tables + stream) for M x N frames."""
+
+    def __init__(self, rp: Radar, device=0, stream=None):
+        self._lib = load()
+        self.radar = rp
+        self.M, self.N = rp.echo_num, rp.range_num
+        h = C.c_void_p()
+        s = C.c_void_p(stream) if stream else None
+        _check(self._lib.isar_create(C.byref(h), C.byref(rp), device, s), "isar_create")
+        self._h = h
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self._lib.isar_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    @property
+    def stream(self):
+        return self._lib.isar_stream(self._h)
+
+    def image_host(self, echo, velocity=None, flags=0):
+        """echo: numpy complex64 [M, N]; returns float32 image [M, 512] (blocking)."""
+        import numpy as np
+        e = np.ascontiguousarray(echo, np.complex64)
+        if e.shape != (self.M, self.N):
+            raise IsarError("echo shape %s != (%d, %d)" % (e.shape, self.M, self.N))
+        v = None if velocity is None else np.ascontiguousarray(velocity, np.float64)
+        img = np.empty((self.M, RANGE_NUM_CUT), np.float32)
+        _check(self._lib.isar_image_host(self._h, e.ctypes.data, None if v is None else v.ctypes.data, flags,
+                                         img.ctypes.data), "isar_image_host")
+        return img
+
+    def image_device(self, d_echo, d_velocity, d_img, flags=0):
+        _check(self._lib.isar_image_device(self._h, _dptr(d_echo), _dptr(d_velocity), flags, _dptr(d_img)),
+               "isar_image_device")
+
+    def profiles_ptr(self):
+        p = C.c_void_p()
+        _check(self._lib.isar_get_profiles(self._h, C.byref(p)), "isar_get_profiles")
+        return p.value
+
+    def trace(self):
+        import numpy as np
+        sh = np.zeros(self.M - 1, np.float32)
+        ph = np.zeros(self.M, np.complex64)
+        t = Trace()
+        t.ra_shift = sh.ctypes.data
+        t.phase = ph.ctypes.data
+        _check(self._lib.isar_get_trace(self._h, C.byref(t)), "isar_get_trace")
+        U = t.unit2_num
+        return dict(ra_shift=sh, phase=ph, center_applied=t.center_applied, center_shift=t.center_shift,
+                    cut_offset=t.cut_offset, center_idx1_len=t.center_idx1_len,
+                    center_idx2_len=t.center_idx2_len, center_threshold=t.center_threshold,
+                    tgt_num=t.tgt_num, unit2_num=U, bins=np.array(t.bins[:min(U, 512)], np.int32))
+
+    # stage entry points (device buffers, stream-ordered)
+    def stage_hpc(self, d_x, d_vel):
+        _check(self._lib.isar_stage_hpc(self._h, _dptr(d_x), _dptr(d_vel)), "isar_stage_hpc")
+
+    def stage_range_align(self, d_x, d_vel=None, flags=0):
+        _check(self._lib.isar_stage_range_align(self._h, _dptr(d_x), _dptr(d_vel), flags),
+               "isar_stage_range_align")
+
+    def stage_center_cut(self, d_y, d_cut):
+        _check(self._lib.isar_stage_center_cut(self._h, _dptr(d_y), _dptr(d_cut)), "isar_stage_center_cut")
+
+    def stage_fast_entropy(self, d_cut, iterations=120):
+        _check(self._lib.isar_stage_fast_entropy(self._h, _dptr(d_cut), iterations), "isar_stage_fast_entropy")
+
+    def stage_post(self, d_cut, d_img, flags=0):
+        _check(self._lib.isar_stage_post(self._h, _dptr(d_cut), flags, _dptr(d_img)), "isar_stage_post")
+
+    def fft_rows(self, d_x, rows, n, inverse=False):
+        _check(self._lib.isar_fft_rows(self._h, _dptr(d_x), rows, n, 1 if inverse else 0), "isar_fft_rows")

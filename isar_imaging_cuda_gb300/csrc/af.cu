@@ -1,0 +1,458 @@
+// Doppler tracking and fast minimum-entropy autofocus on the M x 512 cut.
+// Reference: phase_adjustment.cu:4-41 (dopplerTracking), :167-332
+// (fastEntropy), common.cu:341-391 (maxCols/sumCols), :436-462 (sumRows).
+#include <cuda_runtime.h>
+#include <math_constants.h>
+
+#include "fft.cuh"
+#include "isar_kernels.h"
+
+namespace isar {
+
+constexpr int C = kRangeCut;
+
+// Column max of |cut| over rows [0, min(M,256)) per CTA of R rows, and the
+// Doppler sums s[m] = sum_c conj(x[m,c]) x[m+1,c] (one warp per row).
+__global__ void __launch_bounds__(256)
+k_fe_stats(const float2* __restrict__ cut, int M, int rows_max, int R, float* __restrict__ cmax_part,
+           float2* __restrict__ dsum)
+{
+    const int r0 = blockIdx.x * R;
+    const int tid = threadIdx.x;
+    if (cmax_part != nullptr && r0 < rows_max) {
+        const int r1 = min(r0 + R, rows_max);
+        for (int c = tid; c < C; c += blockDim.x) {
+            float mx = 0.0f;
+            for (int r = r0; r < r1; ++r) {
+                const float2 v = cut[(size_t)r * C + c];
+                mx = fmaxf(mx, sqrtf(v.x * v.x + v.y * v.y));
+            }
+            cmax_part[(size_t)blockIdx.x * C + c] = mx;
+        }
+    }
+    const int w = tid >> 5, lane = tid & 31;
+    for (int m = r0 + w; m < min(r0 + R, M - 1); m += blockDim.x >> 5) {
+        float2 s = make_float2(0.0f, 0.0f);
+        for (int c = lane; c < C; c += 32) {
+            const float2 a = cut[(size_t)m * C + c];
+            const float2 b = cut[(size_t)(m + 1) * C + c];
+            const float2 p = cmulc(a, b);
+            s.x += p.x;
+            s.y += p.y;
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            s.x += __shfl_xor_sync(0xffffffffu, s.x, o);
+            s.y += __shfl_xor_sync(0xffffffffu, s.y, o);
+        }
+        if (lane == 0) dsum[m] = s;
+    }
+}
+
+// Same Doppler sums on the U gathered bins: s[m] = sum_u conj(g[m,u]) g[m+1,u].
+__global__ void __launch_bounds__(256)
+k_af_doppler(const float2* __restrict__ cut, const int* __restrict__ bins, const int* __restrict__ fdec,
+             int M, float2* __restrict__ dsum)
+{
+    const int U = fdec[1];
+    const int w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+    const int m = w;
+    if (m >= M - 1) return;
+    float2 s = make_float2(0.0f, 0.0f);
+    for (int u = lane; u < U; u += 32) {
+        const int b = bins[u];
+        const float2 p = cmulc(cut[(size_t)m * C + b], cut[(size_t)(m + 1) * C + b]);
+        s.x += p.x;
+        s.y += p.y;
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        s.x += __shfl_xor_sync(0xffffffffu, s.x, o);
+        s.y += __shfl_xor_sync(0xffffffffu, s.y, o);
+    }
+    if (lane == 0) dsum[m] = s;
+}
+
+// One CTA (1024 threads).  Optional target count (phase_adjustment.cu:180-194):
+// colmax, mean with an int accumulator (Q3), threshold 1.48*mean.  Then the
+// Doppler phase: psi = arg(s), Phi = inclusive scan, phase[0] = 0,
+// phase[m+1] = exp(-j*Phi[m]) (phase_adjustment.cu:17-31).
+// fdec: [0] tgt_num, [1] U.
+__global__ void __launch_bounds__(1024)
+k_fe_phase(const float* __restrict__ cmax_part, int nparts, const float2* __restrict__ dsum, int M,
+           float2* __restrict__ phase, int* __restrict__ fdec)
+{
+    __shared__ double sc[1024];
+    __shared__ int s_cnt[32];
+    __shared__ long long s_sum[32];
+    const int tid = threadIdx.x;
+    const int lane = tid & 31, w = tid >> 5;
+    if (nparts > 0) {
+        float mx = 0.0f;
+        int iv = 0;
+        if (tid < C) {
+            for (int p = 0; p < nparts; ++p) mx = fmaxf(mx, cmax_part[(size_t)p * C + tid]);
+            iv = (int)mx;
+        }
+        long long sum = iv;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) sum += __shfl_xor_sync(0xffffffffu, sum, o);
+        if (lane == 0) s_sum[w] = sum;
+        __syncthreads();
+        if (tid == 0) {
+            long long t = 0;
+            for (int i = 0; i < 32; ++i) t += s_sum[i];
+            s_sum[0] = t;
+        }
+        __syncthreads();
+        const float mean_val = (float)(int)s_sum[0] / (float)C;
+        const float thr = 1.48f * mean_val;
+        int cnt = (tid < C && mx > thr) ? 1 : 0;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) cnt += __shfl_xor_sync(0xffffffffu, cnt, o);
+        if (lane == 0) s_cnt[w] = cnt;
+        __syncthreads();
+        if (tid == 0) {
+            int t = 0;
+            for (int i = 0; i < 32; ++i) t += s_cnt[i];
+            // U = nextPow2(tgt_num / 2) (common.cu:521-529)
+            int n = t / 2, u = 1;
+            while (n >> 1) {
+                u <<= 1;
+                n >>= 1;
+            }
+            fdec[0] = t;
+            fdec[1] = u << 1;
+        }
+    }
+    // inclusive scan of arg(s) in double
+    double v = 0.0;
+    if (tid < M - 1) {
+        const float2 s = dsum[tid];
+        v = (double)atan2f(s.y, s.x);
+    }
+    sc[tid] = v;
+    __syncthreads();
+    for (int o = 1; o < 1024; o <<= 1) {
+        double add = (tid >= o) ? sc[tid - o] : 0.0;
+        __syncthreads();
+        sc[tid] += add;
+        __syncthreads();
+    }
+    if (tid == 0) phase[0] = make_float2(0.0f, 0.0f);
+    if (tid < M - 1) {
+        double sn, cs;
+        sincos(sc[tid], &sn, &cs);
+        phase[tid + 1] = make_float2((float)cs, (float)-sn);
+    }
+}
+
+// team reduction (sum) of a double over the T threads of a team.
+template <int T>
+__device__ __forceinline__ double team_sum(double v, int lt, double* red /* per-team, >= T/32 */)
+{
+    if constexpr (T >= 32) {
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+        constexpr int W = T / 32;
+        if constexpr (W > 1) {
+            if ((lt & 31) == 0) red[lt >> 5] = v;
+            __syncthreads();
+            double t = 0.0;
+#pragma unroll
+            for (int i = 0; i < W; ++i) t += red[i];
+            __syncthreads();
+            return t;
+        }
+        return v;
+    } else {
+#pragma unroll
+        for (int o = T / 2; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o, T);
+        return v;
+    }
+}
+
+// Per column: FFT over pulses of phase[m]*cut[m,c], energy E = sum |X|^2 and
+// entropy H = -sum p ln p, p = |X|^2/E (phase_adjustment.cu:215-246).
+// CB columns per CTA, one team of M/16 threads per column.
+template <int M, int CB>
+__global__ void __launch_bounds__(CB * M / 16)
+k_fe_colfft(const float2* __restrict__ cut, const float2* __restrict__ phase, double* __restrict__ E,
+            double* __restrict__ H, const float2* __restrict__ tw)
+{
+    using F = FFTShape<M>;
+    extern __shared__ float4 dyn_smem[];
+    float2* smb = reinterpret_cast<float2*>(dyn_smem);
+    __shared__ double red[CB][(F::T + 31) / 32];
+    const int tid = threadIdx.x;
+    const int team = tid / F::T, lt = tid % F::T;
+    const int c0 = blockIdx.x * CB;
+    for (int i = tid; i < M * CB; i += blockDim.x) {
+        const int m = i / CB, cc = i % CB;
+        smb[cc * F::SMEM + fpad(m)] = cmul(phase[m], cut[(size_t)m * C + c0 + cc]);
+    }
+    __syncthreads();
+    float2* sm = smb + team * F::SMEM;
+    float p[16];
+    team_fft<M, false>([&](int i) { return sm[fpad(i)]; },
+                       [&](int, float2 v, int slot) { p[slot] = v.x * v.x + v.y * v.y; }, sm, lt, tw);
+    double e = 0.0;
+#pragma unroll
+    for (int q = 0; q < 16; ++q) e += (double)p[q];
+    e = team_sum<F::T>(e, lt, red[team]);
+    const float ef = (float)e;
+    double h = 0.0;
+#pragma unroll
+    for (int q = 0; q < 16; ++q) {
+        const float x = p[q] / ef;
+        h += (double)(-(x * logf(x)));
+    }
+    h = team_sum<F::T>(h, lt, red[team]);
+    if (lt == 0) {
+        E[c0 + team] = e;
+        H[c0 + team] = h;
+    }
+}
+
+// Bin selection (phase_adjustment.cu:248-264), one CTA of 512 threads:
+// stable sort by energy (descending), keep tgt_num, stable sort by entropy
+// (ascending), keep U (indices beyond tgt_num are 0, as device_vector::resize
+// pads), sort the kept indices.  NaN keys sort last.
+__global__ void __launch_bounds__(512)
+k_fe_select(const double* __restrict__ E, const double* __restrict__ H, int* __restrict__ fdec,
+            int* __restrict__ bins)
+{
+    __shared__ double key[C];
+    __shared__ int id[C];
+    __shared__ int pos[C];
+    const int tid = threadIdx.x;
+    const int tgt = fdec[0], U = fdec[1];
+    {
+        double e = E[tid];
+        key[tid] = isnan(e) ? -CUDART_INF : e;
+        id[tid] = tid;
+    }
+    __syncthreads();
+    // bitonic: "a before b" iff key_a > key_b or (== and id_a < id_b)
+    for (int k = 2; k <= C; k <<= 1)
+        for (int j = k >> 1; j > 0; j >>= 1) {
+            const int i = tid, ixj = i ^ j;
+            if (ixj > i) {
+                const bool up = (i & k) == 0;
+                const double ka = key[i], kb = key[ixj];
+                const int ia = id[i], ib = id[ixj];
+                const bool a_first = (ka > kb) || (ka == kb && ia < ib);
+                if (a_first != up) {
+                    key[i] = kb;
+                    key[ixj] = ka;
+                    id[i] = ib;
+                    id[ixj] = ia;
+                }
+            }
+            __syncthreads();
+        }
+    // second key: entropy of the first tgt entries; the rest are sentinels
+    {
+        const int i = tid;
+        double h = (i < tgt) ? H[id[i]] : CUDART_INF;
+        if (isnan(h)) h = CUDART_INF;
+        const int sel = id[i];
+        __syncthreads();
+        key[i] = h;
+        pos[i] = (i < tgt) ? i : (C + i);
+        id[i] = sel;
+    }
+    __syncthreads();
+    for (int k = 2; k <= C; k <<= 1)
+        for (int j = k >> 1; j > 0; j >>= 1) {
+            const int i = tid, ixj = i ^ j;
+            if (ixj > i) {
+                const bool up = (i & k) == 0;
+                const double ka = key[i], kb = key[ixj];
+                const int pa = pos[i], pb = pos[ixj];
+                const bool a_first = (ka < kb) || (ka == kb && pa < pb);
+                if (a_first != up) {
+                    key[i] = kb;
+                    key[ixj] = ka;
+                    pos[i] = pb;
+                    pos[ixj] = pa;
+                    const int t = id[i];
+                    id[i] = id[ixj];
+                    id[ixj] = t;
+                }
+            }
+            __syncthreads();
+        }
+    // keep U, pad with 0, sort ascending
+    {
+        const int i = tid;
+        int b = 0x7fffffff;
+        if (i < U) b = (i < tgt) ? id[i] : 0;
+        __syncthreads();
+        pos[i] = b;
+    }
+    __syncthreads();
+    for (int k = 2; k <= C; k <<= 1)
+        for (int j = k >> 1; j > 0; j >>= 1) {
+            const int i = tid, ixj = i ^ j;
+            if (ixj > i) {
+                const bool up = (i & k) == 0;
+                const int a = pos[i], b = pos[ixj];
+                if ((a > b) == up) {
+                    pos[i] = b;
+                    pos[ixj] = a;
+                }
+            }
+            __syncthreads();
+        }
+    if (tid < U) bins[tid] = pos[tid];
+}
+
+// gT[u][m] = cut[m][bins[u]] for u < U (transposed so that each bin is a
+// contiguous FFT input).
+__global__ void k_af_gather(const float2* __restrict__ cut, const int* __restrict__ bins,
+                            const int* __restrict__ fdec, int M, float2* __restrict__ gT)
+{
+    const int U = fdec[1];
+    const int u = blockIdx.y;
+    if (u >= U) return;
+    const int b = bins[u];
+    for (int m = blockIdx.x * blockDim.x + threadIdx.x; m < M; m += gridDim.x * blockDim.x)
+        gT[(size_t)u * M + m] = cut[(size_t)m * C + b];
+}
+
+// One minimum-entropy iteration (phase_adjustment.cu:302-318) on CB bins per
+// CTA: t = phase .* g; T = FFT(t); T .* |T|; h = IFFT(T)/M; q = conj(g) .* h;
+// per-CTA partial row sums sig_part[cta][m] = sum over the CTA's bins of q.
+template <int M, int CB>
+__global__ void __launch_bounds__(CB * M / 16)
+k_af_iter(const float2* __restrict__ gT, const float2* __restrict__ phase, const int* __restrict__ fdec,
+          float2* __restrict__ sig_part, const float2* __restrict__ tw)
+{
+    using F = FFTShape<M>;
+    extern __shared__ float4 dyn_smem[];
+    float2* smb = reinterpret_cast<float2*>(dyn_smem);
+    const int U = fdec[1];
+    const int u0 = blockIdx.x * CB;
+    if (u0 >= U) return;
+    const int tid = threadIdx.x;
+    const int team = tid / F::T, lt = tid % F::T;
+    const int u = u0 + team;
+    const bool valid = u < U;
+    const float2* g = gT + (size_t)u * M;
+    float2* sm = smb + team * F::SMEM;
+    const float invM = 1.0f / (float)M;
+    team_fft<M, false>(
+        [&](int i) { return valid ? cmul(phase[i], g[i]) : make_float2(0.0f, 0.0f); },
+        [&](int i, float2 v, int) {
+            const float a = sqrtf(v.x * v.x + v.y * v.y);
+            sm[fpad(i)] = cscale(v, a);
+        },
+        sm, lt, tw);
+    team_fft<M, true>([&](int i) { return sm[fpad(i)]; },
+                      [&](int i, float2 v, int) {
+                          const float2 h = cscale(v, invM);
+                          sm[fpad(i)] = valid ? cmulc(g[i], h) : make_float2(0.0f, 0.0f);
+                      },
+                      sm, lt, tw);
+    __syncthreads();
+    for (int m = tid; m < M; m += blockDim.x) {
+        float2 s = make_float2(0.0f, 0.0f);
+#pragma unroll
+        for (int t = 0; t < CB; ++t) {
+            const float2 q = smb[t * F::SMEM + fpad(m)];
+            s.x += q.x;
+            s.y += q.y;
+        }
+        sig_part[(size_t)blockIdx.x * M + m] = s;
+    }
+}
+
+// phase[m] = sigma[m] / |sigma[m]|, sigma = sum of the partials.
+__global__ void k_af_norm(const float2* __restrict__ sig_part, const int* __restrict__ fdec, int CB, int M,
+                          float2* __restrict__ phase)
+{
+    const int U = fdec[1];
+    const int np = (U + CB - 1) / CB;
+    for (int m = blockIdx.x * blockDim.x + threadIdx.x; m < M; m += gridDim.x * blockDim.x) {
+        float2 s = make_float2(0.0f, 0.0f);
+        for (int p = 0; p < np; ++p) {
+            const float2 q = sig_part[(size_t)p * M + m];
+            s.x += q.x;
+            s.y += q.y;
+        }
+        const float a = sqrtf(s.x * s.x + s.y * s.y);
+        phase[m] = make_float2(s.x / a, s.y / a);
+    }
+}
+
+// cut[m][c] *= phase[m]  (phase_adjustment.cu:324)
+__global__ void k_af_apply(float2* __restrict__ cut, const float2* __restrict__ phase, int M)
+{
+    const int m = blockIdx.x;
+    const float2 p = phase[m];
+    for (int c = threadIdx.x; c < C; c += blockDim.x) cut[(size_t)m * C + c] = cmul(p, cut[(size_t)m * C + c]);
+}
+
+// ---------------------------------------------------------------------------
+// host side
+// ---------------------------------------------------------------------------
+template <int M>
+static constexpr int af_cb() { return M >= 512 ? 8 : (M >= 256 ? 16 : 32); }
+
+template <int M>
+static cudaError_t fe_run_m(const FEArgs& a, cudaStream_t st)
+{
+    constexpr int CB = af_cb<M>();
+    using F = FFTShape<M>;
+    const size_t smem = (size_t)CB * F::SMEM * sizeof(float2);
+    static bool attr = false;
+    if (!attr) {
+        cudaError_t e;
+        if ((e = cudaFuncSetAttribute(k_fe_colfft<M, CB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)))
+            return e;
+        if ((e = cudaFuncSetAttribute(k_af_iter<M, CB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)))
+            return e;
+        attr = true;
+    }
+    const int rows_max = M < 256 ? M : 256;
+    const int R = 8;
+    const int nparts = (rows_max + R - 1) / R;
+    k_fe_stats<<<(M + R - 1) / R, 256, 0, st>>>(a.cut, M, rows_max, R, a.cmax_part, a.dsum);
+    ISAR_COUNT(1);
+    k_fe_phase<<<1, 1024, 0, st>>>(a.cmax_part, nparts, a.dsum, M, a.phase, a.fdec);
+    ISAR_COUNT(1);
+    k_fe_colfft<M, CB><<<C / CB, CB * F::T, smem, st>>>(a.cut, a.phase, a.E, a.H, a.tw);
+    ISAR_COUNT(1);
+    k_fe_select<<<1, C, 0, st>>>(a.E, a.H, a.fdec, a.bins);
+    ISAR_COUNT(1);
+    dim3 gg((M + 255) / 256, C);
+    k_af_gather<<<gg, 256, 0, st>>>(a.cut, a.bins, a.fdec, M, a.gT);
+    ISAR_COUNT(1);
+    k_af_doppler<<<(M * 32 + 255) / 256, 256, 0, st>>>(a.cut, a.bins, a.fdec, M, a.dsum);
+    ISAR_COUNT(1);
+    k_fe_phase<<<1, 1024, 0, st>>>(nullptr, 0, a.dsum, M, a.phase, a.fdec);
+    ISAR_COUNT(1);
+    for (int it = 0; it < a.iters; ++it) {
+        k_af_iter<M, CB><<<C / CB, CB * F::T, smem, st>>>(a.gT, a.phase, a.fdec, a.sig_part, a.tw);
+        ISAR_COUNT(1);
+        k_af_norm<<<(M + 255) / 256, 256, 0, st>>>(a.sig_part, a.fdec, CB, M, a.phase);
+        ISAR_COUNT(1);
+    }
+    k_af_apply<<<M, 256, 0, st>>>(a.cut, a.phase, M);
+    ISAR_COUNT(1);
+    return cudaGetLastError();
+}
+
+cudaError_t fe_run(const FEArgs& a, cudaStream_t st)
+{
+    switch (a.M) {
+    case 128: return fe_run_m<128>(a, st);
+    case 256: return fe_run_m<256>(a, st);
+    case 512: return fe_run_m<512>(a, st);
+    case 1024: return fe_run_m<1024>(a, st);
+    default: return cudaErrorInvalidValue;
+    }
+}
+
+}  // namespace isar

@@ -1,0 +1,165 @@
+// Block-level FFT engine: power-of-two complex64 FFTs held in shared memory
+// and registers.  A "team" of N/16 threads owns one transform; a CTA may run
+// several teams side by side (each with its own shared-memory slice), all in
+// lockstep.
+//
+// Algorithm: Stockham auto-sort, radix-16 passes followed by one radix-2/4/8
+// pass when log2(N) is not a multiple of 4.  Pass p with radix R and
+// Ns = product of the earlier radices maps j in [0, N/R), k = j mod Ns:
+//   a[r]  = in[j + r*N/R]
+//   a[r] *= W_{Ns*R}^{r*k}                                  (twiddle table)
+//   a     = DFT_R(a)                                        (registers)
+//   out[(j/Ns)*Ns*R + k + r*Ns] = a[r]
+// The first pass reads through a caller functor (fused pre-multiply), the last
+// pass hands each output (index, value, register slot) to a caller functor
+// (fused epilogue).  Shared-memory slots are padded by one element every 16
+// to keep the stride-16 writes of the first pass conflict free.
+//
+// Conventions as cuFFT: forward = exp(-i), inverse = exp(+i), unnormalised.
+#pragma once
+
+#include "isar_common.cuh"
+
+namespace isar {
+
+__host__ __device__ constexpr int ilog2c(int n) { return n <= 1 ? 0 : 1 + ilog2c(n >> 1); }
+
+__device__ __forceinline__ int fpad(int i) { return i + (i >> 4); }
+
+template <int N>
+struct FFTShape {
+    static constexpr int T = N / 16;                 // threads per team
+    static constexpr int LOG = ilog2c(N);
+    static constexpr int NP16 = LOG / 4;             // radix-16 passes
+    static constexpr int REM = LOG % 4;
+    static constexpr int NPASS = NP16 + (REM ? 1 : 0);
+    static constexpr int SMEM = N + N / 16;          // float2 slots per team
+};
+
+// d * exp(-+2*pi*i*j/R) with j, R compile-time after unrolling (R <= 16).
+template <bool INV>
+__device__ __forceinline__ float2 twc_mul(float2 d, int j, int R)
+{
+    const int k16 = j * (16 / R);   // angle = 2*pi*k16/16, k16 in [0, 8)
+    const float c1 = 0.92387953251128674f, c2 = 0.70710678118654752f, c3 = 0.38268343236508977f;
+    float c, s;
+    switch (k16) {
+    case 0: return d;
+    case 4: return INV ? make_float2(-d.y, d.x) : make_float2(d.y, -d.x);
+    case 1: c = c1; s = c3; break;
+    case 2: c = c2; s = c2; break;
+    case 3: c = c3; s = c1; break;
+    case 5: c = -c3; s = c1; break;
+    case 6: c = -c2; s = c2; break;
+    default: c = -c1; s = c3; break;   // 7
+    }
+    // forward: (c - i s), inverse: (c + i s)
+    if (INV) return make_float2(d.x * c - d.y * s, d.x * s + d.y * c);
+    return make_float2(d.x * c + d.y * s, d.y * c - d.x * s);
+}
+
+// In-register DFT of length R (2..16): radix-2 decimation in frequency, then
+// the bit-reversal permutation (register renaming after unrolling).
+template <int R, bool INV>
+__device__ __forceinline__ void dft_reg(float2* a)
+{
+#pragma unroll
+    for (int len = R; len >= 2; len >>= 1) {
+        const int half = len >> 1;
+#pragma unroll
+        for (int s = 0; s < R; s += len) {
+#pragma unroll
+            for (int k = 0; k < half; ++k) {
+                float2 u = a[s + k], v = a[s + k + half];
+                a[s + k] = cadd(u, v);
+                a[s + k + half] = twc_mul<INV>(csub(u, v), k * (R / len), R);
+            }
+        }
+    }
+    float2 b[R];
+#pragma unroll
+    for (int i = 0; i < R; ++i) b[i] = a[i];
+    constexpr int L = ilog2c(R);
+#pragma unroll
+    for (int i = 0; i < R; ++i) {
+        int r = 0;
+#pragma unroll
+        for (int q = 0; q < L; ++q) r |= ((i >> q) & 1) << (L - 1 - q);
+        a[i] = b[r];
+    }
+}
+
+template <int N, int R, int NS, bool INV, bool FIRST, bool LAST, class Src, class Dst>
+__device__ __forceinline__ void fft_pass(Src& src, Dst& dst, float2* sm, int lt, const float2* __restrict__ tw)
+{
+    constexpr int T = N / 16;
+    constexpr int B = 16 / R;
+    float2 v[16];
+#pragma unroll
+    for (int b = 0; b < B; ++b) {
+        const int j = lt + b * T;
+#pragma unroll
+        for (int r = 0; r < R; ++r) {
+            const int idx = j + r * (N / R);
+            if constexpr (FIRST) v[b * R + r] = src(idx);
+            else v[b * R + r] = sm[fpad(idx)];
+        }
+    }
+    __syncthreads();
+#pragma unroll
+    for (int b = 0; b < B; ++b) {
+        const int j = lt + b * T;
+        const int k = j & (NS - 1);
+        if constexpr (NS > 1) {
+#pragma unroll
+            for (int r = 1; r < R; ++r) {
+                float2 w = __ldg(&tw[(r * k) * (kTwN / (NS * R))]);
+                if (INV) w.y = -w.y;
+                v[b * R + r] = cmul(v[b * R + r], w);
+            }
+        }
+        dft_reg<R, INV>(&v[b * R]);
+        const int base = (j / NS) * NS * R + k;
+#pragma unroll
+        for (int r = 0; r < R; ++r) {
+            const int idx = base + r * NS;
+            if constexpr (LAST) dst(idx, v[b * R + r], b * R + r);
+            else sm[fpad(idx)] = v[b * R + r];
+        }
+    }
+    __syncthreads();
+}
+
+template <int N, bool INV, int PASS, int NS, class Src, class Dst>
+__device__ __forceinline__ void fft_passes(Src& src, Dst& dst, float2* sm, int lt, const float2* __restrict__ tw)
+{
+    using S = FFTShape<N>;
+    constexpr int R = (PASS < S::NP16) ? 16 : (1 << S::REM);
+    fft_pass<N, R, NS, INV, PASS == 0, PASS == S::NPASS - 1>(src, dst, sm, lt, tw);
+    if constexpr (PASS + 1 < S::NPASS) fft_passes<N, INV, PASS + 1, NS * R>(src, dst, sm, lt, tw);
+}
+
+// One team transform.  src(i) -> float2 for i in [0,N) (first pass, may read
+// global memory); dst(i, v, slot) receives output i (slot in [0,16) is the
+// register slot, fixed per thread and output index).  sm: this team's slice
+// of FFTShape<N>::SMEM float2.  lt: thread index within the team.
+// Contains __syncthreads(): every thread of the CTA must call it.
+template <int N, bool INV, class Src, class Dst>
+__device__ __forceinline__ void team_fft(Src src, Dst dst, float2* sm, int lt, const float2* __restrict__ tw)
+{
+    static_assert(N >= 32 && (N & (N - 1)) == 0 && N <= kTwN, "FFT size");
+    fft_passes<N, INV, 0, 1>(src, dst, sm, lt, tw);
+}
+
+// Output index of register slot `slot` for thread lt (the LAST pass mapping),
+// so that callers can revisit their outputs after the transform.
+template <int N>
+__device__ __forceinline__ int fft_out_index(int lt, int slot)
+{
+    using S = FFTShape<N>;
+    constexpr int R = (S::NPASS - 1 < S::NP16) ? 16 : (1 << S::REM);
+    const int b = slot / R, r = slot % R;
+    return lt + b * S::T + r * (N / R);
+}
+
+}  // namespace isar

@@ -1,0 +1,79 @@
+// Internal launcher interface between the host pipeline and the kernels.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <atomic>
+
+namespace isar {
+
+// Number of kernels this library has launched (all contexts).
+inline std::atomic<long long>& launch_counter()
+{
+    static std::atomic<long long> n{0};
+    return n;
+}
+#define ISAR_COUNT(n) (::isar::launch_counter() += (n))
+
+struct RAArgs {
+    int M, N;
+    const float2* x;         // [M][N] spectra in
+    float2* y;               // [M][N] range profiles out (may equal x)
+    const float* win;        // [N] hamming(n) * cos(pi*n), float as the reference
+    const int64_t* hq;       // [M] HPC phase coefficient (fixed point) or nullptr
+    double* S;               // [M] cumulative alignment shift, cells
+    float* shifts;           // [M-1] per (level, pair) shift, level-major
+    float* env_a;            // [M/2][N] envelope ping buffer
+    float* env_b;            // [M/2][N] envelope pong buffer
+    float* part;             // [max(M/2,256)][N] partial sums
+    float* arp;              // [N] average range profile
+    unsigned* hmax;          // max |y| (float bits)
+    const float2* tw;        // twiddle table exp(-2 pi i k / kTwN)
+    int pair_min;            // use the fused pair kernel while pairs >= pair_min
+    int rpc;                 // rows per CTA for the accumulate kernel
+    int rpc_final;           // rows per CTA for the final transform
+};
+
+struct FEArgs {
+    int M;
+    int iters;
+    float2* cut;             // [M][512], phase applied in place at the end
+    float* cmax_part;        // [ceil(min(M,256)/8)][512]
+    float2* dsum;            // [M]
+    float2* phase;           // [M]
+    int* fdec;               // [0] tgt_num, [1] U
+    double* E;               // [512]
+    double* H;               // [512]
+    int* bins;               // [512]
+    float2* gT;              // [512][M]
+    float2* sig_part;        // [512/CB][M]
+    const float2* tw;
+};
+
+struct PostArgs {
+    int M;
+    int data_type;           // 1 IFDS, 2 STRETCH
+    int mtrc;
+    float2* cut;             // [M][512]
+    float2* st;              // [M][512] scratch
+    float2* st2;             // [M][512] scratch
+    const float2* pre;       // [M][512] a^-k * ww[M-1+k]
+    const float2* post;      // [M][512] ww[M-1+k]
+    const float2* V;         // [512][L] FFT_L(1/ww)
+    const float* hamM;       // [M]
+    float* img;              // [M][512]
+    const float2* tw;
+};
+
+cudaError_t hpc_coef(const double* vel, int M, double coef_over_fs2, int64_t* hq, cudaStream_t st);
+cudaError_t hpc_apply(float2* x, const int64_t* hq, int M, int N, cudaStream_t st);
+cudaError_t ifds_pre(float2* x, int M, int N, const float2* tw, cudaStream_t st);
+cudaError_t ra_run(const RAArgs& a, cudaStream_t st);
+cudaError_t arp_from_y(const float2* y, int M, int N, float* tmp, unsigned* hmax, float* arp, cudaStream_t st);
+cudaError_t center_cut(const float* arp, const float2* y, int M, int N, int* dec, float2* cut, cudaStream_t st);
+cudaError_t fe_run(const FEArgs& a, cudaStream_t st);
+cudaError_t post_run(const PostArgs& a, cudaStream_t st);
+cudaError_t fft_rows(float2* x, int rows, int n, int inverse, const float2* tw, cudaStream_t st);
+
+}  // namespace isar

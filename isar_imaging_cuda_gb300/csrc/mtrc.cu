@@ -1,0 +1,211 @@
+// CZT-based MTRC correction and image formation on the M x 512 cut.
+// Reference: mtrc.cu:4-76 (mtrc), :125-172 (cztRange, Bluestein),
+// isar_main.cu:191-211 (post-processing).
+#include <cuda_runtime.h>
+
+#include "fft.cuh"
+#include "isar_kernels.h"
+
+namespace isar {
+
+constexpr int C = kRangeCut;
+
+// Rows: ifftshift then IFFT/512 (STRETCH) or FFT (IFDS) (mtrc.cu:18-40).
+template <bool INV>
+__global__ void __launch_bounds__(256) k_mtrc_rows(const float2* __restrict__ cut, float2* __restrict__ st,
+                                                   const float2* __restrict__ tw)
+{
+    using F = FFTShape<C>;
+    __shared__ float2 smb[8 * F::SMEM];
+    const int team = threadIdx.x / F::T, lt = threadIdx.x % F::T;
+    const int m = blockIdx.x * 8 + team;
+    const float2* xr = cut + (size_t)m * C;
+    float2* o = st + (size_t)m * C;
+    const float sc = INV ? 1.0f / (float)C : 1.0f;
+    team_fft<C, INV>([&](int i) { return xr[(i + C / 2) & (C - 1)]; },
+                     [&](int i, float2 v, int) { o[i] = cscale(v, sc); }, smb + team * F::SMEM, lt, tw);
+}
+
+// Bluestein CZT along pulses for CB range bins (mtrc.cu:125-172):
+// y = pre .* x (zero padded to L), Y = FFT_L(y) .* V, y = IFFT_L(Y)/L,
+// out[k] = y[M-1+k] * post[k].
+template <int M, int CB>
+__global__ void __launch_bounds__(CB * (2 * M) / 16)
+k_czt(const float2* __restrict__ st, const float2* __restrict__ pre, const float2* __restrict__ post,
+      const float2* __restrict__ V, float2* __restrict__ out, const float2* __restrict__ tw)
+{
+    constexpr int L = 2 * M;
+    using F = FFTShape<L>;
+    extern __shared__ float4 dyn_smem[];
+    float2* smb = reinterpret_cast<float2*>(dyn_smem);
+    float2* tile = smb + CB * F::SMEM;   // [M][CB]
+    const int tid = threadIdx.x;
+    const int team = tid / F::T, lt = tid % F::T;
+    const int c0 = blockIdx.x * CB;
+    for (int i = tid; i < M * CB; i += blockDim.x) {
+        const int k = i / CB, cc = i % CB;
+        const size_t g = (size_t)k * C + c0 + cc;
+        tile[i] = cmul(pre[g], st[g]);
+    }
+    __syncthreads();
+    float2* sm = smb + team * F::SMEM;
+    const int c = c0 + team;
+    const float2* Vc = V + (size_t)c * L;
+    const float invL = 1.0f / (float)L;
+    team_fft<L, false>([&](int i) { return i < M ? tile[i * CB + team] : make_float2(0.0f, 0.0f); },
+                       [&](int i, float2 v, int) { sm[fpad(i)] = cmul(v, Vc[i]); }, sm, lt, tw);
+    team_fft<L, true>([&](int i) { return sm[fpad(i)]; },
+                      [&](int i, float2 v, int) {
+                          const int k = i - (M - 1);
+                          if (k >= 0 && k < M) tile[k * CB + team] = cscale(v, invL);
+                      },
+                      sm, lt, tw);
+    __syncthreads();
+    for (int i = tid; i < M * CB; i += blockDim.x) {
+        const int k = i / CB, cc = i % CB;
+        const size_t g = (size_t)k * C + c0 + cc;
+        out[g] = cmul(tile[i], post[g]);
+    }
+}
+
+// Columns: ifftshift, IFFT/M, ifftshift (mtrc.cu:53-61).
+template <int M, int CB>
+__global__ void __launch_bounds__(CB * M / 16)
+k_mtrc_cols(const float2* __restrict__ in, float2* __restrict__ out, const float2* __restrict__ tw)
+{
+    using F = FFTShape<M>;
+    extern __shared__ float4 dyn_smem[];
+    float2* smb = reinterpret_cast<float2*>(dyn_smem);
+    const int tid = threadIdx.x;
+    const int team = tid / F::T, lt = tid % F::T;
+    const int c0 = blockIdx.x * CB;
+    for (int i = tid; i < M * CB; i += blockDim.x) {
+        const int m = i / CB, cc = i % CB;
+        smb[cc * F::SMEM + fpad(m)] = in[(size_t)((m + M / 2) & (M - 1)) * C + c0 + cc];
+    }
+    __syncthreads();
+    float2* sm = smb + team * F::SMEM;
+    const float invM = 1.0f / (float)M;
+    team_fft<M, true>([&](int i) { return sm[fpad(i)]; },
+                      [&](int i, float2 v, int) { sm[fpad((i + M / 2) & (M - 1))] = cscale(v, invM); }, sm, lt,
+                      tw);
+    __syncthreads();
+    for (int i = tid; i < M * CB; i += blockDim.x) {
+        const int m = i / CB, cc = i % CB;
+        out[(size_t)m * C + c0 + cc] = smb[cc * F::SMEM + fpad(m)];
+    }
+}
+
+// Rows: FFT(512), fftshift (mtrc.cu:63-66); IFDS adds fliplr (:72-75).
+__global__ void __launch_bounds__(256) k_mtrc_rowfft(const float2* __restrict__ in, float2* __restrict__ out,
+                                                     int fliplr, const float2* __restrict__ tw)
+{
+    using F = FFTShape<C>;
+    __shared__ float2 smb[8 * F::SMEM];
+    const int team = threadIdx.x / F::T, lt = threadIdx.x % F::T;
+    const int m = blockIdx.x * 8 + team;
+    const float2* xr = in + (size_t)m * C;
+    float2* o = out + (size_t)m * C;
+    team_fft<C, false>([&](int i) { return xr[i]; },
+                       [&](int i, float2 v, int) {
+                           int d = (i + C / 2) & (C - 1);
+                           if (fliplr) d = C - 1 - d;
+                           o[d] = v;
+                       },
+                       smb + team * F::SMEM, lt, tw);
+}
+
+// Post-processing per column: (optional column fftshift of the input),
+// Hamming over pulses, FFT over pulses, fftshift, (IFDS: flipud), |.|.
+template <int M, int CB>
+__global__ void __launch_bounds__(CB * M / 16)
+k_post(const float2* __restrict__ cut, int src_shift, const float* __restrict__ hamM, int flipud,
+       float* __restrict__ img, const float2* __restrict__ tw)
+{
+    using F = FFTShape<M>;
+    extern __shared__ float4 dyn_smem[];
+    float2* smb = reinterpret_cast<float2*>(dyn_smem);
+    float* tile = reinterpret_cast<float*>(smb + CB * F::SMEM);   // [M][CB]
+    const int tid = threadIdx.x;
+    const int team = tid / F::T, lt = tid % F::T;
+    const int c0 = blockIdx.x * CB;
+    for (int i = tid; i < M * CB; i += blockDim.x) {
+        const int m = i / CB, cc = i % CB;
+        const float2 v = cut[(size_t)((m + src_shift) & (M - 1)) * C + c0 + cc];
+        smb[cc * F::SMEM + fpad(m)] = cscale(v, hamM[m]);
+    }
+    __syncthreads();
+    float2* sm = smb + team * F::SMEM;
+    team_fft<M, false>([&](int i) { return sm[fpad(i)]; },
+                       [&](int i, float2 v, int) {
+                           int r = (i + M / 2) & (M - 1);
+                           if (flipud) r = M - 1 - r;
+                           tile[r * CB + team] = sqrtf(v.x * v.x + v.y * v.y);
+                       },
+                       sm, lt, tw);
+    __syncthreads();
+    for (int i = tid; i < M * CB; i += blockDim.x) {
+        const int m = i / CB, cc = i % CB;
+        img[(size_t)m * C + c0 + cc] = tile[i];
+    }
+}
+
+template <int M>
+static constexpr int col_cb() { return M >= 512 ? 8 : (M >= 256 ? 16 : 32); }
+template <int M>
+static constexpr int czt_cb() { return M >= 512 ? 4 : (M >= 256 ? 8 : 16); }
+
+template <int M>
+static cudaError_t post_run_m(const PostArgs& a, cudaStream_t st)
+{
+    constexpr int CB = col_cb<M>();
+    constexpr int CZ = czt_cb<M>();
+    using F = FFTShape<M>;
+    using FL = FFTShape<2 * M>;
+    const size_t smem_post = (size_t)CB * F::SMEM * sizeof(float2) + (size_t)M * CB * sizeof(float);
+    const size_t smem_cols = (size_t)CB * F::SMEM * sizeof(float2);
+    const size_t smem_czt = (size_t)CZ * FL::SMEM * sizeof(float2) + (size_t)M * CZ * sizeof(float2);
+    static bool attr = false;
+    if (!attr) {
+        cudaError_t e;
+        if ((e = cudaFuncSetAttribute(k_post<M, CB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_post)))
+            return e;
+        if ((e = cudaFuncSetAttribute(k_mtrc_cols<M, CB>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      (int)smem_cols)))
+            return e;
+        if ((e = cudaFuncSetAttribute(k_czt<M, CZ>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_czt)))
+            return e;
+        attr = true;
+    }
+    int src_shift = 0;
+    const float2* src = a.cut;
+    if (a.mtrc) {
+        if (a.data_type == 1) k_mtrc_rows<false><<<M / 8, 256, 0, st>>>(a.cut, a.st, a.tw);
+        else k_mtrc_rows<true><<<M / 8, 256, 0, st>>>(a.cut, a.st, a.tw);
+        ISAR_COUNT(1);
+        k_czt<M, CZ><<<C / CZ, CZ * FL::T, smem_czt, st>>>(a.st, a.pre, a.post, a.V, a.st2, a.tw);
+        ISAR_COUNT(1);
+        k_mtrc_cols<M, CB><<<C / CB, CB * F::T, smem_cols, st>>>(a.st2, a.st, a.tw);
+        ISAR_COUNT(1);
+        k_mtrc_rowfft<<<M / 8, 256, 0, st>>>(a.st, a.st2, a.data_type == 1, a.tw);
+        ISAR_COUNT(1);
+        src = a.st2;
+        src_shift = M / 2;   // final column fftshift of mtrc (mtrc.cu:69)
+    }
+    k_post<M, CB><<<C / CB, CB * F::T, smem_post, st>>>(src, src_shift, a.hamM, a.data_type == 1, a.img, a.tw);
+    ISAR_COUNT(1);
+    return cudaGetLastError();
+}
+
+cudaError_t post_run(const PostArgs& a, cudaStream_t st)
+{
+    switch (a.M) {
+    case 128: return post_run_m<128>(a, st);
+    case 256: return post_run_m<256>(a, st);
+    case 512: return post_run_m<512>(a, st);
+    case 1024: return post_run_m<1024>(a, st);
+    default: return cudaErrorInvalidValue;
+    }
+}
+
+}  // namespace isar

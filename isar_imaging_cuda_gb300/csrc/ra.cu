@@ -1,0 +1,785 @@
+// Range alignment (with fused high-speed compensation), HRRP centering and
+// range cut.  Reference: range_alignment.cu:4-78 (rangeAlignmentParallel),
+// high_speed_compensation.cu:4-54, range_alignment.cu:371-465 (HRRPCenter),
+// common.cu:494-518 (cutRangeProfile).
+//
+// Formulation.  The reference keeps the data x[m,n] (range spectra) in HBM and,
+// at every level of its binary merge, IFFTs all M rows, forms group RMS
+// envelopes, correlates neighbouring groups and multiplies the second group
+// by a linear phase ramp.  Here x is never rewritten: every row carries a
+// cumulative shift S_m (cells) and a high-speed-compensation coefficient, and
+// each load applies window * exp(j*2*pi*(alpha_m*n^2 - S_m*n/N)) on the fly
+// (64-bit fixed-point phase, exact modulo one cycle).  Rows of the first half
+// of a group are unchanged since the previous level, so their envelope is
+// carried over ("left" vector) and only the rows shifted by the previous
+// level are transformed again: (log2 M - 1) * M/2 + 2M row FFTs instead of
+// (log2 M + 1) * M.
+#include <cuda_runtime.h>
+
+#include "fft.cuh"
+#include "isar_kernels.h"
+
+namespace isar {
+
+__device__ __forceinline__ int64_t frac_to_fixed(double f)
+{
+    f -= floor(f + 0.5);   // [-0.5, 0.5)
+    return (int64_t)llrint(ldexp(f, 64));
+}
+
+__device__ __forceinline__ float2 row_phase(int64_t hq, int64_t sq, int n)
+{
+    const uint64_t nn = (uint64_t)n;
+    const uint64_t ph = (uint64_t)hq * (nn * nn) - (uint64_t)sq * nn;
+    return cis_frac64(ph);
+}
+
+// HPC coefficient per pulse: alpha_m = coef * v_m / Fs^2 in cycles per n^2,
+// coef = -4*pi*(B/Tp)/c (high_speed_compensation.cu:17-18).
+__global__ void k_hpc_coef(const double* __restrict__ vel, int M, double coef_over_fs2, int64_t* __restrict__ hq)
+{
+    int m = blockIdx.x * blockDim.x + threadIdx.x;
+    if (m < M) {
+        double cyc = coef_over_fs2 * vel[m] / 6.283185307179586476925;
+        hq[m] = frac_to_fixed(cyc);
+    }
+}
+
+__global__ void k_zero_d(double* __restrict__ p, int n)
+{
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) p[i] = 0.0;
+}
+
+// Standalone HPC (stage test entry): x *= exp(j*2*pi*alpha_m*n^2).
+__global__ void k_hpc_apply(float2* __restrict__ x, const int64_t* __restrict__ hq, int N)
+{
+    const int m = blockIdx.y;
+    const int64_t h = hq[m];
+    for (int n = blockIdx.x * blockDim.x + threadIdx.x; n < N; n += gridDim.x * blockDim.x) {
+        float2 v = x[(size_t)m * N + n];
+        x[(size_t)m * N + n] = cmul(v, row_phase(h, 0, n));
+    }
+}
+
+// Block-wide argmax (ArgKey order) over one value per thread slot.
+template <int T>
+__device__ __forceinline__ ArgKey block_argmax(ArgKey k, ArgKey* red)
+{
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        ArgKey y;
+        y.a = __shfl_xor_sync(0xffffffffu, k.a, o);
+        y.i = __shfl_xor_sync(0xffffffffu, k.i, o);
+        if (argkey_better(y, k)) k = y;
+    }
+    constexpr int W = T / 32;
+    if constexpr (W > 1) {
+        const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+        if (lane == 0) red[w] = k;
+        __syncthreads();
+        if (w == 0) {
+            k = (lane < W) ? red[lane] : red[0];
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) {
+                ArgKey y;
+                y.a = __shfl_xor_sync(0xffffffffu, k.a, o);
+                y.i = __shfl_xor_sync(0xffffffffu, k.i, o);
+                if (argkey_better(y, k)) k = y;
+            }
+            if (lane == 0) red[0] = k;
+        }
+        __syncthreads();
+        k = red[0];
+        __syncthreads();
+    }
+    return k;
+}
+
+// Correlates the RMS envelopes sqrt(ea) and sqrt(eb) as
+// C2R(R2C(a) .* conj(R2C(b))) -> ifftshift -> argmax|.| -> parabolic fix
+// (range_alignment.cu:50-66, :121-168) and returns the shift (all threads).
+// ea and eb are adjacent N-float shared arrays; they are overwritten.
+template <int N>
+__device__ float ra_correlate(float* ea, float* sm_f, int lt, const float2* __restrict__ tw)
+{
+    using F = FFTShape<N>;
+    constexpr int T = F::T;
+    float2* sm = reinterpret_cast<float2*>(sm_f);
+    float* eb = ea + N;
+    float2* zb = reinterpret_cast<float2*>(ea);
+    __shared__ ArgKey red[32];
+    __shared__ float s_res;
+    // z = a + i b, forward FFT into zb
+    team_fft<N, false>([&](int i) { return make_float2(sqrtf(ea[i]), sqrtf(eb[i])); },
+                       [&](int i, float2 v, int) { zb[i] = v; }, sm, lt, tw);
+    // C[k] = A[k] * conj(B[k]) with A, B split from Z; corr = IFFT(C) real part
+    float* corr = ea;
+    team_fft<N, true>(
+        [&](int k) {
+            const float2 zk = zb[k];
+            const float2 zn = zb[(N - k) & (N - 1)];
+            const float2 a = make_float2(0.5f * (zk.x + zn.x), 0.5f * (zk.y - zn.y));
+            const float2 d = make_float2(zk.x - zn.x, zk.y + zn.y);
+            const float2 bc = make_float2(0.5f * d.y, 0.5f * d.x);   // conj(B), B = -i d / 2
+            return cmul(a, bc);
+        },
+        [&](int i, float2 v, int) { corr[i] = v.x; }, sm, lt, tw);
+    // argmax over the ifftshifted correlation
+    ArgKey best;
+    best.a = -1.0f;
+    best.i = 0x7fffffff;
+#pragma unroll 4
+    for (int t = 0; t < N / T; ++t) {
+        const int i = lt + t * T;
+        ArgKey k;
+        k.a = fabsf(corr[(i + N / 2) & (N - 1)]);
+        k.i = i;
+        if (argkey_better(k, best)) best = k;
+    }
+    best = block_argmax<T>(best, red);
+    if (lt == 0) {
+        const int pos = best.i;
+        const float f1 = corr[((pos - 1) + N / 2) & (N - 1)];
+        const float f2 = corr[(pos + N / 2) & (N - 1)];
+        const float f3 = corr[((pos + 1) + N / 2) & (N - 1)];
+        const float fa = (f1 + f3 - 2 * f2) / 2;
+        const float fb = (f3 - f1) / 2;
+        s_res = (float)pos + (-fb / (2 * fa)) - (float)N / 2;
+    }
+    __syncthreads();
+    const float r = s_res;
+    __syncthreads();
+    return r;
+}
+
+// One row: IFFT(x * win * exp(j 2 pi (alpha n^2 - S n / N))) / N, |.|^2
+// accumulated into acc (register slots of this thread).
+template <int N>
+__device__ __forceinline__ void ra_row_power(const float2* __restrict__ xr, const float* __restrict__ win,
+                                             int64_t h, int64_t sq, float* acc, float2* sm, int lt,
+                                             const float2* __restrict__ tw)
+{
+    const float invN = 1.0f / (float)N;
+    team_fft<N, true>(
+        [&](int i) {
+            const float2 v = xr[i];
+            return cscale(cmul(v, row_phase(h, sq, i)), __ldg(&win[i]));
+        },
+        [&](int, float2 v, int slot) {
+            const float re = v.x * invN, im = v.y * invN;
+            acc[slot] += re * re + im * im;
+        },
+        sm, lt, tw);
+}
+
+// Level kernel, one CTA per pair j of groups (G_2j, G_2j+1) of size s=2^level.
+// Level 0 transforms both rows; level >= 1 transforms the second halves R_k
+// of both groups and adds the carried envelopes left_prev[k] of the first
+// halves.  Writes the pair shift, adds it to S of the rows of G_2j+1 and
+// stores env^2(G_2j) as left_next[j].
+template <int N>
+__global__ void __launch_bounds__(N / 16)
+k_ra_pair(const float2* __restrict__ x, const float* __restrict__ win, const int64_t* __restrict__ hq,
+          double* __restrict__ S, int level, const float* __restrict__ left_prev, int lstride,
+          float* __restrict__ left_next, float* __restrict__ shift_out, const float2* __restrict__ tw)
+{
+    using F = FFTShape<N>;
+    extern __shared__ float4 dyn_smem[];
+    float* sm_f = reinterpret_cast<float*>(dyn_smem);
+    float* ea = sm_f + 2 * F::SMEM;
+    float* eb = ea + N;
+    const int lt = threadIdx.x;
+    const int s = 1 << level;
+    const int j = blockIdx.x;
+    float2* sm = reinterpret_cast<float2*>(sm_f);
+#pragma unroll 1
+    for (int g = 0; g < 2; ++g) {
+        const int k = 2 * j + g;
+        const int r0 = (level == 0) ? k : k * s + s / 2;
+        const int nr = (level == 0) ? 1 : s / 2;
+        float acc[16];
+#pragma unroll
+        for (int q = 0; q < 16; ++q) acc[q] = 0.0f;
+#pragma unroll 1
+        for (int rr = 0; rr < nr; ++rr) {
+            const int row = r0 + rr;
+            const int64_t h = hq ? hq[row] : 0;
+            const int64_t sq = frac_to_fixed(S[row] / (double)N);
+            ra_row_power<N>(x + (size_t)row * N, win, h, sq, acc, sm, lt, tw);
+        }
+        float* e = g ? eb : ea;
+#pragma unroll
+        for (int q = 0; q < 16; ++q) {
+            const int i = fft_out_index<N>(lt, q);
+            float v = acc[q];
+            if (level > 0) v += left_prev[(size_t)k * lstride * N + i];
+            e[i] = v;
+        }
+    }
+    __syncthreads();
+    if (left_next)
+        for (int i = lt; i < N; i += F::T) left_next[(size_t)j * N + i] = ea[i];
+    __syncthreads();
+    const float sh = ra_correlate<N>(ea, sm_f, lt, tw);
+    if (lt == 0) shift_out[j] = sh;
+    for (int m = lt; m < s; m += F::T) S[(size_t)(2 * j + 1) * s + m] += (double)sh;
+}
+
+// Level >= 1, many rows per group: CTA b transforms rpc rows of R_k
+// (k = b / nch, chunk q = b % nch) and writes their summed |p|^2.
+template <int N>
+__global__ void __launch_bounds__(N / 16)
+k_ra_accum(const float2* __restrict__ x, const float* __restrict__ win, const int64_t* __restrict__ hq,
+           const double* __restrict__ S, int level, int rpc, float* __restrict__ part,
+           const float2* __restrict__ tw)
+{
+    using F = FFTShape<N>;
+    extern __shared__ float4 dyn_smem[];
+    float2* sm = reinterpret_cast<float2*>(dyn_smem);
+    const int lt = threadIdx.x;
+    const int s = 1 << level;
+    const int nch = (s / 2) / rpc;
+    const int k = blockIdx.x / nch, q = blockIdx.x % nch;
+    const int r0 = k * s + s / 2 + q * rpc;
+    float acc[16];
+#pragma unroll
+    for (int t = 0; t < 16; ++t) acc[t] = 0.0f;
+#pragma unroll 1
+    for (int rr = 0; rr < rpc; ++rr) {
+        const int row = r0 + rr;
+        const int64_t h = hq ? hq[row] : 0;
+        const int64_t sq = frac_to_fixed(S[row] / (double)N);
+        ra_row_power<N>(x + (size_t)row * N, win, h, sq, acc, sm, lt, tw);
+    }
+#pragma unroll
+    for (int t = 0; t < 16; ++t) part[(size_t)blockIdx.x * N + fft_out_index<N>(lt, t)] = acc[t];
+}
+
+// E[k] = left_prev[k * lstride] + sum of the nch partials of R_k.
+__global__ void k_ra_reduce(const float* __restrict__ left_prev, int lstride, const float* __restrict__ part,
+                            int nch, int N, float* __restrict__ E)
+{
+    const int k = blockIdx.y;
+    for (int n = blockIdx.x * blockDim.x + threadIdx.x; n < N; n += gridDim.x * blockDim.x) {
+        float v = left_prev[(size_t)k * lstride * N + n];
+        for (int q = 0; q < nch; ++q) v += part[((size_t)k * nch + q) * N + n];
+        E[(size_t)k * N + n] = v;
+    }
+}
+
+// Pair correlation on materialised envelopes E[2j], E[2j+1].
+template <int N>
+__global__ void __launch_bounds__(N / 16)
+k_ra_corr(const float* __restrict__ E, double* __restrict__ S, int level, float* __restrict__ shift_out,
+          const float2* __restrict__ tw)
+{
+    using F = FFTShape<N>;
+    extern __shared__ float4 dyn_smem[];
+    float* sm_f = reinterpret_cast<float*>(dyn_smem);
+    float* ea = sm_f + 2 * F::SMEM;
+    const int lt = threadIdx.x;
+    const int j = blockIdx.x;
+    const int s = 1 << level;
+    for (int i = lt; i < 2 * N; i += F::T) ea[i] = E[(size_t)2 * j * N + i];
+    __syncthreads();
+    const float sh = ra_correlate<N>(ea, sm_f, lt, tw);
+    if (lt == 0) shift_out[j] = sh;
+    for (int m = lt; m < s; m += F::T) S[(size_t)(2 * j + 1) * s + m] += (double)sh;
+}
+
+// Final transform of all rows, written in place: y = IFFT(x*win*ramp)/N.
+// Epilogue: column sums of |y| over rows < min(M,256) per CTA (ARP partials)
+// and the global max |y| (HRRPCenter normalisation, range_alignment.cu:380-399).
+template <int N>
+__global__ void __launch_bounds__(N / 16)
+k_ra_final(const float2* x, float2* yout, const float* __restrict__ win, const int64_t* __restrict__ hq,
+           const double* __restrict__ S, int rpc, int arp_rows, float* __restrict__ arp_part,
+           unsigned* __restrict__ hmax, const float2* __restrict__ tw)
+{
+    using F = FFTShape<N>;
+    extern __shared__ float4 dyn_smem[];
+    float2* sm = reinterpret_cast<float2*>(dyn_smem);
+    __shared__ float s_red[32];
+    const int lt = threadIdx.x;
+    const int r0 = blockIdx.x * rpc;
+    const float invN = 1.0f / (float)N;
+    float acc[16];
+#pragma unroll
+    for (int t = 0; t < 16; ++t) acc[t] = 0.0f;
+    float mx = 0.0f;
+#pragma unroll 1
+    for (int rr = 0; rr < rpc; ++rr) {
+        const int row = r0 + rr;
+        const int64_t h = hq ? hq[row] : 0;
+        const int64_t sq = frac_to_fixed(S[row] / (double)N);
+        const float2* xr = x + (size_t)row * N;
+        float2* yr = yout + (size_t)row * N;
+        const bool arp = row < arp_rows;
+        team_fft<N, true>(
+            [&](int i) { return cscale(cmul(xr[i], row_phase(h, sq, i)), __ldg(&win[i])); },
+            [&](int i, float2 v, int slot) {
+                const float2 y = make_float2(v.x * invN, v.y * invN);
+                yr[i] = y;
+                const float a = sqrtf(y.x * y.x + y.y * y.y);
+                mx = fmaxf(mx, a);
+                if (arp) acc[slot] += a;
+            },
+            sm, lt, tw);
+    }
+    if (r0 < arp_rows) {
+#pragma unroll
+        for (int t = 0; t < 16; ++t) arp_part[(size_t)blockIdx.x * N + fft_out_index<N>(lt, t)] = acc[t];
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+    if ((lt & 31) == 0) s_red[lt >> 5] = mx;
+    __syncthreads();
+    if (lt == 0) {
+        float m = 0.0f;
+        for (int w = 0; w < (F::T + 31) / 32; ++w) m = fmaxf(m, s_red[w]);
+        atomicMax(hmax, __float_as_uint(m));
+    }
+}
+
+// ARP[n] = (sum_p part[p][n]) * (1/hmax) * (1/M)   (range_alignment.cu:388-399)
+__global__ void k_arp_reduce(const float* __restrict__ part, int nparts, int N, int M,
+                             const unsigned* __restrict__ hmax, float* __restrict__ arp)
+{
+    const float inv = 1.0f / __uint_as_float(*hmax);
+    const float invM = 1.0f / (float)M;
+    for (int n = blockIdx.x * blockDim.x + threadIdx.x; n < N; n += gridDim.x * blockDim.x) {
+        float s = 0.0f;
+        for (int p = 0; p < nparts; ++p) s += part[(size_t)p * N + n];
+        arp[n] = (s * inv) * invM;
+    }
+}
+
+// Standalone ARP inputs from materialised profiles y (stage entry point).
+__global__ void k_ymax(const float2* __restrict__ y, long n, unsigned* __restrict__ hmax)
+{
+    float mx = 0.0f;
+    for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) {
+        const float2 v = y[i];
+        mx = fmaxf(mx, sqrtf(v.x * v.x + v.y * v.y));
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+    if ((threadIdx.x & 31) == 0) atomicMax(hmax, __float_as_uint(mx));
+}
+
+__global__ void k_ycolsum(const float2* __restrict__ y, int N, int rows, float* __restrict__ colsum)
+{
+    for (int n = blockIdx.x * blockDim.x + threadIdx.x; n < N; n += gridDim.x * blockDim.x) {
+        float s = 0.0f;
+        for (int m = 0; m < rows; ++m) {
+            const float2 v = y[(size_t)m * N + n];
+            s += sqrtf(v.x * v.x + v.y * v.y);
+        }
+        colsum[n] = s;
+    }
+}
+
+// getARPMean (range_alignment.cu:524-550) for one index, float as written.
+__device__ __forceinline__ float arp_mean(const float* arp, int idx, int WL, int N)
+{
+    float s = 0.0f;
+    if (idx - WL / 2 >= 0 && idx + WL / 2 <= N - 1) {
+        for (int i = idx - WL / 2; i <= idx + WL / 2; ++i) s += arp[i];
+        s /= (float)(WL + 1);
+    } else if (idx - WL / 2 < 0) {
+        for (int i = 0; i <= idx + WL / 2; ++i) s += arp[i];
+        s /= ((float)WL / 2 + idx + 1);
+    } else if (idx + WL / 2 > N - 1) {
+        for (int i = idx - WL / 2; i < N; ++i) s += arp[i];
+        s /= ((float)N - idx - ((float)WL / 2) - 1);
+    }
+    return s;
+}
+
+template <class T>
+__device__ __forceinline__ T block_sum_1024(T v, T* red)
+{
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    if (lane == 0) red[w] = v;
+    __syncthreads();
+    if (w == 0) {
+        v = (lane < (int)(blockDim.x >> 5)) ? red[lane] : (T)0;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+        if (lane == 0) red[0] = v;
+    }
+    __syncthreads();
+    v = red[0];
+    __syncthreads();
+    return v;
+}
+
+// HRRPCenter decisions + cutRangeProfile offset, one CTA of 1024 threads.
+// dec: [0] applied, [1] shift_num, [2] cut offset, [3] |idx_1|, [4] |idx_2|,
+//      [5] threshold (float bits).
+__global__ void __launch_bounds__(1024)
+k_center(const float* __restrict__ arp_g, const float2* __restrict__ y, int N, int inter_length,
+         int* __restrict__ dec)
+{
+    extern __shared__ float4 dyn_smem[];
+    float* arp = reinterpret_cast<float*>(dyn_smem);
+    float* srt = arp + N;
+    __shared__ long long red_ll[32];
+    __shared__ int red_i[32];
+    __shared__ float red_f[32];
+    __shared__ int red_j[32];
+    const int tid = threadIdx.x;
+    for (int i = tid; i < N; i += blockDim.x) {
+        const float v = arp_g[i];
+        arp[i] = v;
+        srt[i] = v;
+    }
+    __syncthreads();
+    // bitonic sort ascending (thrust::stable_sort of arp1, :404)
+    for (int k = 2; k <= N; k <<= 1) {
+        for (int jj = k >> 1; jj > 0; jj >>= 1) {
+            for (int i = tid; i < N; i += blockDim.x) {
+                const int ixj = i ^ jj;
+                if (ixj > i) {
+                    const bool up = (i & k) == 0;
+                    const float a = srt[i], b = srt[ixj];
+                    if ((a > b) == up) {
+                        srt[i] = b;
+                        srt[ixj] = a;
+                    }
+                }
+            }
+            __syncthreads();
+        }
+    }
+    // extra = inter_length * max(arp1) / N ; diff argmin (first index) (:406-420)
+    const float arp1_max = srt[N - 1];
+    const float extra = (float)inter_length * arp1_max / (float)N;
+    const int dl = N - inter_length;
+    float bv = 3.4e38f;
+    int bi = 0x7fffffff;
+    for (int i = tid; i < dl; i += blockDim.x) {
+        const float d = fabsf(srt[i + inter_length] - srt[i] - extra);
+        if (d < bv || (d == bv && i < bi)) {
+            bv = d;
+            bi = i;
+        }
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        const float ov = __shfl_xor_sync(0xffffffffu, bv, o);
+        const int oi = __shfl_xor_sync(0xffffffffu, bi, o);
+        if (ov < bv || (ov == bv && oi < bi)) {
+            bv = ov;
+            bi = oi;
+        }
+    }
+    if ((tid & 31) == 0) {
+        red_f[tid >> 5] = bv;
+        red_j[tid >> 5] = bi;
+    }
+    __syncthreads();
+    if (tid == 0) {
+        float v = red_f[0];
+        int ii = red_j[0];
+        for (int w = 1; w < (int)(blockDim.x >> 5); ++w)
+            if (red_f[w] < v || (red_f[w] == v && red_j[w] < ii)) {
+                v = red_f[w];
+                ii = red_j[w];
+            }
+        red_j[0] = ii;
+    }
+    __syncthreads();
+    const int dmin = red_j[0];
+    __syncthreads();
+    const float thr = srt[dmin + inter_length / 2];
+    // idx_1 = find(arp > thr); drop those whose 9-tap mean < thr (:426-449)
+    int n1 = 0, n2 = 0;
+    long long sum = 0;
+    for (int n = tid; n < N; n += blockDim.x) {
+        if (arp[n] > thr) {
+            ++n1;
+            if (arp_mean(arp, n, 8, N) < thr) ++n2;
+            else sum += n;
+        }
+    }
+    n1 = block_sum_1024<int>(n1, red_i);
+    n2 = block_sum_1024<int>(n2, red_i);
+    sum = block_sum_1024<long long>(sum, red_ll);
+    int applied = 0, shift = 0;
+    if (n2 != n1) {
+        const int mean_idx = (int)(sum / (long long)(n1 - n2));
+        shift = -(mean_idx - N / 2);
+        applied = 1;
+    }
+    // cutRangeProfile: Icamax (|Re|+|Im|, first max) of centred row 0
+    float cv = -1.0f;
+    int ci = 0x7fffffff;
+    for (int n = tid; n < N; n += blockDim.x) {
+        const float2 v = y[(n - shift) & (N - 1)];
+        const float a = fabsf(v.x) + fabsf(v.y);
+        if (a > cv) {
+            cv = a;
+            ci = n;
+        }
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        const float ov = __shfl_xor_sync(0xffffffffu, cv, o);
+        const int oi = __shfl_xor_sync(0xffffffffu, ci, o);
+        if (ov > cv || (ov == cv && oi < ci)) {
+            cv = ov;
+            ci = oi;
+        }
+    }
+    if ((tid & 31) == 0) {
+        red_f[tid >> 5] = cv;
+        red_j[tid >> 5] = ci;
+    }
+    __syncthreads();
+    if (tid == 0) {
+        float v = red_f[0];
+        int ii = red_j[0];
+        for (int w = 1; w < (int)(blockDim.x >> 5); ++w)
+            if (red_f[w] > v || (red_f[w] == v && red_j[w] < ii)) {
+                v = red_f[w];
+                ii = red_j[w];
+            }
+        int off = ii - kRangeCut / 2;
+        if (off < 0) off = 0;
+        if (off > N - kRangeCut) off = N - kRangeCut;
+        dec[0] = applied;
+        dec[1] = shift;
+        dec[2] = off;
+        dec[3] = n1;
+        dec[4] = n2;
+        dec[5] = __float_as_int(thr);
+    }
+}
+
+// cut[m][c] = centred y[m][off + c] = y[m][(off + c - shift) mod N]
+__global__ void k_cut(const float2* __restrict__ y, int N, const int* __restrict__ dec, float2* __restrict__ cut)
+{
+    const int m = blockIdx.x;
+    const int shift = dec[1], off = dec[2];
+    for (int c = threadIdx.x; c < kRangeCut; c += blockDim.x)
+        cut[(size_t)m * kRangeCut + c] = y[(size_t)m * N + ((off + c - shift) & (N - 1))];
+}
+
+// IFDS pre-step (isar_main.cu:15-27): ifftshift, IFFT/N, ifftshift per row.
+template <int N>
+__global__ void __launch_bounds__(N / 16) k_ifds_pre(float2* x, const float2* __restrict__ tw)
+{
+    using F = FFTShape<N>;
+    extern __shared__ float4 dyn_smem[];
+    float2* sm = reinterpret_cast<float2*>(dyn_smem);
+    float2* xr = x + (size_t)blockIdx.x * N;
+    const float invN = 1.0f / (float)N;
+    team_fft<N, true>([&](int i) { return xr[(i + N / 2) & (N - 1)]; },
+                      [&](int i, float2 v, int) { xr[(i + N / 2) & (N - 1)] = cscale(v, invN); },
+                      sm, threadIdx.x, tw);
+}
+
+// Test entry: batched row FFTs of length N (unnormalised).
+template <int N, bool INV>
+__global__ void __launch_bounds__(N / 16) k_fft_rows(float2* x, const float2* __restrict__ tw)
+{
+    using F = FFTShape<N>;
+    extern __shared__ float4 dyn_smem[];
+    float2* sm = reinterpret_cast<float2*>(dyn_smem);
+    float2* xr = x + (size_t)blockIdx.x * N;
+    team_fft<N, INV>([&](int i) { return xr[i]; }, [&](int i, float2 v, int) { xr[i] = v; }, sm, threadIdx.x, tw);
+}
+
+// ---------------------------------------------------------------------------
+// host launchers
+// ---------------------------------------------------------------------------
+template <int N>
+static size_t pair_smem() { return (size_t)FFTShape<N>::SMEM * sizeof(float2) + 2 * N * sizeof(float); }
+template <int N>
+static size_t fft_smem() { return (size_t)FFTShape<N>::SMEM * sizeof(float2); }
+
+template <int N>
+static cudaError_t set_attrs()
+{
+    static bool done = false;
+    if (done) return cudaSuccess;
+    cudaError_t e;
+    const int big = (int)pair_smem<N>();
+    if ((e = cudaFuncSetAttribute(k_ra_pair<N>, cudaFuncAttributeMaxDynamicSharedMemorySize, big))) return e;
+    if ((e = cudaFuncSetAttribute(k_ra_corr<N>, cudaFuncAttributeMaxDynamicSharedMemorySize, big))) return e;
+    const int f = (int)fft_smem<N>();
+    if ((e = cudaFuncSetAttribute(k_ra_accum<N>, cudaFuncAttributeMaxDynamicSharedMemorySize, f))) return e;
+    if ((e = cudaFuncSetAttribute(k_ra_final<N>, cudaFuncAttributeMaxDynamicSharedMemorySize, f))) return e;
+    if ((e = cudaFuncSetAttribute(k_ifds_pre<N>, cudaFuncAttributeMaxDynamicSharedMemorySize, f))) return e;
+    if ((e = cudaFuncSetAttribute(k_fft_rows<N, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, f))) return e;
+    if ((e = cudaFuncSetAttribute(k_fft_rows<N, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, f))) return e;
+    done = true;
+    return cudaSuccess;
+}
+
+template <int N>
+static cudaError_t ra_run_n(const RAArgs& a, cudaStream_t st)
+{
+    cudaError_t e = set_attrs<N>();
+    if (e) return e;
+    const int M = a.M;
+    const int T = N / 16;
+    int L = 0;
+    while ((1 << L) < M) ++L;
+    k_zero_d<<<(M + 255) / 256, 256, 0, st>>>(a.S, M);
+    ISAR_COUNT(1);
+    const float* left = nullptr;
+    int lstride = 1;
+    float* bufs[2] = {a.env_a, a.env_b};
+    int cur = 0;
+    int shift_off = 0;
+    for (int lv = 0; lv < L; ++lv) {
+        const int s = 1 << lv;
+        const int pairs = M / (2 * s);
+        const bool last = (lv == L - 1);
+        const bool use_pair = (lv == 0) || pairs >= a.pair_min || (s / 2) <= 1;
+        if (use_pair) {
+            float* ln = last ? nullptr : bufs[cur];
+            k_ra_pair<N><<<pairs, T, pair_smem<N>(), st>>>(a.x, a.win, a.hq, a.S, lv, left, lstride, ln,
+                                                          a.shifts + shift_off, a.tw);
+            ISAR_COUNT(1);
+            left = ln;
+            lstride = 1;
+        } else {
+            int rpc = a.rpc;
+            if (rpc > s / 2) rpc = s / 2;
+            const int nch = (s / 2) / rpc;
+            const int groups = M / s;
+            k_ra_accum<N><<<groups * nch, T, fft_smem<N>(), st>>>(a.x, a.win, a.hq, a.S, lv, rpc, a.part, a.tw);
+            ISAR_COUNT(1);
+            float* E = bufs[cur];
+            dim3 g((N + 255) / 256, groups);
+            k_ra_reduce<<<g, 256, 0, st>>>(left, lstride, a.part, nch, N, E);
+            ISAR_COUNT(1);
+            k_ra_corr<N><<<pairs, T, pair_smem<N>(), st>>>(E, a.S, lv, a.shifts + shift_off, a.tw);
+            ISAR_COUNT(1);
+            left = E;
+            lstride = 2;
+        }
+        cur ^= 1;
+        shift_off += pairs;
+        if ((e = cudaGetLastError())) return e;
+    }
+    // final IFFT + ARP partials + hmax
+    cudaMemsetAsync(a.hmax, 0, sizeof(unsigned), st);
+    const int arp_rows = M < 256 ? M : 256;
+    int rpcf = a.rpc_final;
+    while (rpcf > 1 && (M % rpcf)) rpcf >>= 1;
+    k_ra_final<N><<<M / rpcf, T, fft_smem<N>(), st>>>(a.x, a.y, a.win, a.hq, a.S, rpcf, arp_rows, a.part, a.hmax, a.tw);
+    ISAR_COUNT(1);
+    const int nparts = (arp_rows + rpcf - 1) / rpcf;
+    k_arp_reduce<<<(N + 255) / 256, 256, 0, st>>>(a.part, nparts, N, M, a.hmax, a.arp);
+    ISAR_COUNT(1);
+    return cudaGetLastError();
+}
+
+cudaError_t ra_run(const RAArgs& a, cudaStream_t st)
+{
+    switch (a.N) {
+    case 512: return ra_run_n<512>(a, st);
+    case 1024: return ra_run_n<1024>(a, st);
+    case 2048: return ra_run_n<2048>(a, st);
+    case 4096: return ra_run_n<4096>(a, st);
+    case 8192: return ra_run_n<8192>(a, st);
+    default: return cudaErrorInvalidValue;
+    }
+}
+
+cudaError_t arp_from_y(const float2* y, int M, int N, float* tmp, unsigned* hmax, float* arp, cudaStream_t st)
+{
+    cudaMemsetAsync(hmax, 0, sizeof(unsigned), st);
+    k_ymax<<<1024, 256, 0, st>>>(y, (long)M * N, hmax);
+    ISAR_COUNT(1);
+    k_ycolsum<<<(N + 255) / 256, 256, 0, st>>>(y, N, M < 256 ? M : 256, tmp);
+    ISAR_COUNT(1);
+    k_arp_reduce<<<(N + 255) / 256, 256, 0, st>>>(tmp, 1, N, M, hmax, arp);
+    ISAR_COUNT(1);
+    return cudaGetLastError();
+}
+
+cudaError_t hpc_coef(const double* vel, int M, double coef_over_fs2, int64_t* hq, cudaStream_t st)
+{
+    k_hpc_coef<<<(M + 255) / 256, 256, 0, st>>>(vel, M, coef_over_fs2, hq);
+    ISAR_COUNT(1);
+    return cudaGetLastError();
+}
+
+cudaError_t hpc_apply(float2* x, const int64_t* hq, int M, int N, cudaStream_t st)
+{
+    dim3 g((N + 255) / 256, M);
+    k_hpc_apply<<<g, 256, 0, st>>>(x, hq, N);
+    ISAR_COUNT(1);
+    return cudaGetLastError();
+}
+
+cudaError_t center_cut(const float* arp, const float2* y, int M, int N, int* dec, float2* cut, cudaStream_t st)
+{
+    static bool attr = false;
+    if (!attr) {
+        cudaError_t e = cudaFuncSetAttribute(k_center, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             2 * kMaxN * (int)sizeof(float));
+        if (e) return e;
+        attr = true;
+    }
+    k_center<<<1, 1024, 2 * N * sizeof(float), st>>>(arp, y, N, 30, dec);
+    ISAR_COUNT(1);
+    k_cut<<<M, 256, 0, st>>>(y, N, dec, cut);
+    ISAR_COUNT(1);
+    return cudaGetLastError();
+}
+
+template <int N>
+static cudaError_t ifds_n(float2* x, int M, const float2* tw, cudaStream_t st)
+{
+    cudaError_t e = set_attrs<N>();
+    if (e) return e;
+    k_ifds_pre<N><<<M, N / 16, fft_smem<N>(), st>>>(x, tw);
+    ISAR_COUNT(1);
+    return cudaGetLastError();
+}
+
+cudaError_t ifds_pre(float2* x, int M, int N, const float2* tw, cudaStream_t st)
+{
+    switch (N) {
+    case 512: return ifds_n<512>(x, M, tw, st);
+    case 1024: return ifds_n<1024>(x, M, tw, st);
+    case 2048: return ifds_n<2048>(x, M, tw, st);
+    case 4096: return ifds_n<4096>(x, M, tw, st);
+    case 8192: return ifds_n<8192>(x, M, tw, st);
+    default: return cudaErrorInvalidValue;
+    }
+}
+
+template <int N>
+static cudaError_t fftrows_n(float2* x, int rows, int inverse, const float2* tw, cudaStream_t st)
+{
+    cudaError_t e = set_attrs<N>();
+    if (e) return e;
+    if (inverse) k_fft_rows<N, true><<<rows, N / 16, fft_smem<N>(), st>>>(x, tw);
+    else k_fft_rows<N, false><<<rows, N / 16, fft_smem<N>(), st>>>(x, tw);
+    ISAR_COUNT(1);
+    return cudaGetLastError();
+}
+
+cudaError_t fft_rows(float2* x, int rows, int n, int inverse, const float2* tw, cudaStream_t st)
+{
+    switch (n) {
+    case 512: return fftrows_n<512>(x, rows, inverse, tw, st);
+    case 1024: return fftrows_n<1024>(x, rows, inverse, tw, st);
+    case 2048: return fftrows_n<2048>(x, rows, inverse, tw, st);
+    case 4096: return fftrows_n<4096>(x, rows, inverse, tw, st);
+    case 8192: return fftrows_n<8192>(x, rows, inverse, tw, st);
+    default: return cudaErrorInvalidValue;
+    }
+}
+
+}  // namespace isar

@@ -1,0 +1,146 @@
+"""GPU parity tests: the CUDA path, called through the C ABI, against the FP64
+oracle on the same seeded inputs (stage by stage and whole frames)."""
+import numpy as np
+import pytest
+
+import oracle
+from tests.helpers import make_frame, rel_l2
+
+pytestmark = pytest.mark.gpu
+
+# Tolerances.  FP32 kernels against the FP64 restatement:
+#  - images / profiles: relative L2 <= 1e-4 (the acceptance bar);
+#  - range-alignment shifts: 2e-3 cells (parabolic sub-cell estimate);
+#  - discrete decisions (centering shift, cut offset, bin selection): exact.
+TOL_IMG = 1e-4
+TOL_SHIFT = 2e-3
+
+
+def ctx_for(g, torch, M, N, data_type=oracle.STRETCH):
+    return g.Context(g.radar(M, N, data_type=data_type), stream=torch.cuda.current_stream().cuda_stream)
+
+
+def to_dev(torch, a):
+    return torch.from_numpy(np.ascontiguousarray(a, np.complex64).view(np.float32).copy()).cuda()
+
+
+def from_dev(torch, t):
+    torch.cuda.synchronize()
+    return t.cpu().numpy().view(np.complex64)
+
+
+@pytest.mark.parametrize("n", [512, 1024, 2048, 4096, 8192])
+@pytest.mark.parametrize("inverse", [False, True])
+def test_fft_rows_known_answer(torch_cuda, gb300, n, inverse):
+    torch = torch_cuda
+    rng = np.random.default_rng(n + inverse)
+    x = (rng.standard_normal((3, n)) + 1j * rng.standard_normal((3, n))).astype(np.complex64)
+    with ctx_for(gb300, torch, 128, 512) as ctx:
+        d = to_dev(torch, x)
+        ctx.fft_rows(d, 3, n, inverse)
+        y = from_dev(torch, d).reshape(3, n)
+    want = np.fft.ifft(x.astype(np.complex128), axis=1) * n if inverse else np.fft.fft(x.astype(np.complex128), axis=1)
+    assert rel_l2(y, want) < 2e-6
+
+
+def test_hpc_stage(torch_cuda, gb300):
+    torch = torch_cuda
+    M, N = 128, 1024
+    e, v = make_frame(M, N, seed=21, full=True)
+    rp = oracle.radar(M, N)
+    want = oracle.hpc(e, v, rp)
+    with ctx_for(gb300, torch, M, N) as ctx:
+        d = to_dev(torch, e)
+        dv = torch.from_numpy(v).cuda()
+        ctx.stage_hpc(d, dv)
+        got = from_dev(torch, d).reshape(M, N)
+    assert rel_l2(got, want) < 1e-6
+
+
+@pytest.mark.parametrize("M,N,hpc", [(128, 512, False), (256, 1024, True), (256, 4096, False), (512, 2048, True)])
+def test_range_align_stage(torch_cuda, gb300, M, N, hpc):
+    torch = torch_cuda
+    e, v = make_frame(M, N, seed=M + N, full=hpc)
+    rp = oracle.radar(M, N)
+    x = oracle.hpc(e, v, rp) if hpc else e
+    y_want, sh_want = oracle.range_align(x, rp)
+    with ctx_for(gb300, torch, M, N) as ctx:
+        d = to_dev(torch, e)
+        dv = torch.from_numpy(v).cuda()
+        ctx.stage_range_align(d, dv, gb300.FLAG_HPC if hpc else 0)
+        y = from_dev(torch, d).reshape(M, N)
+        tr = ctx.trace()
+    assert np.max(np.abs(tr["ra_shift"] - sh_want)) < TOL_SHIFT
+    assert rel_l2(y, y_want) < TOL_IMG
+
+
+@pytest.mark.parametrize("M,N", [(128, 1024), (256, 4096)])
+def test_center_cut_stage(torch_cuda, gb300, M, N):
+    torch = torch_cuda
+    e, _ = make_frame(M, N, seed=7 * M + N)
+    rp = oracle.radar(M, N)
+    y, _ = oracle.range_align(e, rp)
+    _, cut_want, tw = oracle.center_cut(y, rp)
+    with ctx_for(gb300, torch, M, N) as ctx:
+        dy = to_dev(torch, y)
+        dc = torch.empty((M, 512 * 2), dtype=torch.float32, device="cuda")
+        ctx.stage_center_cut(dy, dc)
+        cut = from_dev(torch, dc).reshape(M, 512)
+        tr = ctx.trace()
+    for k in ("center_applied", "center_shift", "cut_offset", "center_idx1_len", "center_idx2_len"):
+        assert tr[k] == tw[k], k
+    assert rel_l2(cut, cut_want) < 1e-5
+
+
+@pytest.mark.parametrize("M,N,seed", [(128, 512, 1), (256, 1024, 2), (512, 2048, 3)])
+def test_fast_entropy_stage(torch_cuda, gb300, M, N, seed):
+    torch = torch_cuda
+    e, _ = make_frame(M, N, seed=seed)
+    rp = oracle.radar(M, N)
+    y, _ = oracle.range_align(e, rp)
+    _, cut, _ = oracle.center_cut(y, rp)
+    cut = cut.astype(np.complex64)
+    out_want, tw = oracle.fast_entropy(cut)
+    with ctx_for(gb300, torch, M, N) as ctx:
+        dc = to_dev(torch, cut)
+        ctx.stage_fast_entropy(dc, 120)
+        out = from_dev(torch, dc).reshape(M, 512)
+        tr = ctx.trace()
+    assert tr["tgt_num"] == tw["tgt_num"]
+    assert tr["unit2_num"] == tw["unit2_num"]
+    assert np.array_equal(tr["bins"], tw["bins"])
+    assert rel_l2(out, out_want) < TOL_IMG
+
+
+@pytest.mark.parametrize("M,mtrc", [(128, False), (256, True), (1024, True)])
+def test_post_stage(torch_cuda, gb300, M, mtrc):
+    torch = torch_cuda
+    N = 1024 if M < 1024 else 2048
+    rng = np.random.default_rng(M)
+    cut = (rng.standard_normal((M, 512)) + 1j * rng.standard_normal((M, 512))).astype(np.complex64)
+    rp = oracle.radar(M, N)
+    want = oracle.post(oracle.mtrc(cut, rp) if mtrc else cut)
+    with ctx_for(gb300, torch, M, N) as ctx:
+        dc = to_dev(torch, cut)
+        img = torch.empty((M, 512), dtype=torch.float32, device="cuda")
+        ctx.stage_post(dc, img, gb300.FLAG_MTRC if mtrc else 0)
+        torch.cuda.synchronize()
+        got = img.cpu().numpy()
+    assert rel_l2(got, want) < 1e-5
+
+
+@pytest.mark.parametrize("M,N,full,seed", [(128, 512, False, 31), (256, 4096, False, 32), (256, 2048, True, 33)])
+def test_full_frame(torch_cuda, gb300, M, N, full, seed):
+    torch = torch_cuda
+    e, v = make_frame(M, N, seed=seed, full=full)
+    rp = oracle.radar(M, N)
+    want, tw = oracle.image(e, v, rp, hpc=full, mtrc=full)
+    flags = (gb300.FLAG_HPC | gb300.FLAG_MTRC) if full else 0
+    with ctx_for(gb300, torch, M, N) as ctx:
+        got = ctx.image_host(e, v, flags)
+        tr = ctx.trace()
+    for k in ("center_shift", "cut_offset", "tgt_num", "unit2_num"):
+        assert tr[k] == tw[k], k
+    assert np.array_equal(tr["bins"], tw["bins"])
+    assert rel_l2(got, want) < TOL_IMG
+    assert abs(oracle.entropy(got) - oracle.entropy(want)) < 1e-4
