@@ -117,6 +117,9 @@ __global__ void __launch_bounds__(256) k_mtrc_rowfft(const float2* __restrict__ 
 
 // Post-processing per column: (optional column fftshift of the input),
 // Hamming over pulses, FFT over pulses, fftshift, (IFDS: flipud), |.|.
+// The reference's window launch (isar_main.cu:192) hands diagMulMat
+// cols = echo_num, len = range_num_cut, so only element i < 512 (row 0) is
+// scaled, by hamming[i / echo_num]; the other rows stay unwindowed.
 template <int M, int CB>
 __global__ void __launch_bounds__(CB * M / 16)
 k_post(const float2* __restrict__ cut, int src_shift, const float* __restrict__ hamM, int flipud,
@@ -132,7 +135,7 @@ k_post(const float2* __restrict__ cut, int src_shift, const float* __restrict__ 
     for (int i = tid; i < M * CB; i += blockDim.x) {
         const int m = i / CB, cc = i % CB;
         const float2 v = cut[(size_t)((m + src_shift) & (M - 1)) * C + c0 + cc];
-        smb[cc * F::SMEM + fpad(m)] = cscale(v, hamM[m]);
+        smb[cc * F::SMEM + fpad(m)] = (m == 0) ? cscale(v, hamM[(c0 + cc) / M]) : v;
     }
     __syncthreads();
     float2* sm = smb + team * F::SMEM;

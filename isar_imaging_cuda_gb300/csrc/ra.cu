@@ -96,10 +96,45 @@ __device__ __forceinline__ ArgKey block_argmax(ArgKey k, ArgKey* red)
     return k;
 }
 
-// Correlates the RMS envelopes sqrt(ea) and sqrt(eb) as
-// C2R(R2C(a) .* conj(R2C(b))) -> ifftshift -> argmax|.| -> parabolic fix
-// (range_alignment.cu:50-66, :121-168) and returns the shift (all threads).
-// ea and eb are adjacent N-float shared arrays; they are overwritten.
+// Error-free float accumulation (TwoSum) of the exact product a*b (TwoProd via
+// FMA) into the pair (hi, lo).
+__device__ __forceinline__ void acc_prod(float a, float b, float& hi, float& lo)
+{
+    const float p = a * b;
+    const float e = fmaf(a, b, -p);
+    const float t = hi + p;
+    const float z = t - hi;
+    lo += (hi - (t - z)) + (p - z) + e;
+    hi = t;
+}
+
+template <int T>
+__device__ __forceinline__ double block_sum_d(double v, double* red)
+{
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    constexpr int W = T / 32;
+    if constexpr (W > 1) {
+        const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+        if (lane == 0) red[w] = v;
+        __syncthreads();
+        double t = 0.0;
+#pragma unroll
+        for (int i = 0; i < W; ++i) t += red[i];
+        __syncthreads();
+        v = t;
+    }
+    return v;
+}
+
+// Correlates the RMS envelopes a = sqrt(ea), b = sqrt(eb) as the reference
+// does, C2R(R2C(a) .* conj(R2C(b))) -> ifftshift -> argmax|.| -> parabolic
+// fix (range_alignment.cu:50-66, :121-168), and returns the shift (all
+// threads).  The FFT locates the peak; the three samples of the parabola are
+// then evaluated directly, sum_n a[n] b[n - tau] with error-free float
+// accumulation, because the second difference of a broad correlation peak
+// magnifies FFT rounding into ~1e-4-cell shift errors.  ea, eb are adjacent
+// N-float shared arrays and stay intact; sm_f is the FFT scratch.
 template <int N>
 __device__ float ra_correlate(float* ea, float* sm_f, int lt, const float2* __restrict__ tw)
 {
@@ -107,45 +142,59 @@ __device__ float ra_correlate(float* ea, float* sm_f, int lt, const float2* __re
     constexpr int T = F::T;
     float2* sm = reinterpret_cast<float2*>(sm_f);
     float* eb = ea + N;
-    float2* zb = reinterpret_cast<float2*>(ea);
     __shared__ ArgKey red[32];
+    __shared__ double redd[32];
     __shared__ float s_res;
-    // z = a + i b, forward FFT into zb
+    __shared__ int s_pos;
+    // z = a + i b, forward FFT, spectrum kept in the scratch (padded slots)
     team_fft<N, false>([&](int i) { return make_float2(sqrtf(ea[i]), sqrtf(eb[i])); },
-                       [&](int i, float2 v, int) { zb[i] = v; }, sm, lt, tw);
-    // C[k] = A[k] * conj(B[k]) with A, B split from Z; corr = IFFT(C) real part
-    float* corr = ea;
+                       [&](int i, float2 v, int) { sm[fpad(i)] = v; }, sm, lt, tw);
+    // C[k] = A[k] * conj(B[k]) with A, B split from Z; corr = Re IFFT(C);
+    // argmax over the ifftshifted index (i + N/2) mod N tracked per thread
+    ArgKey best;
+    best.a = -1.0f;
+    best.i = 0x7fffffff;
     team_fft<N, true>(
         [&](int k) {
-            const float2 zk = zb[k];
-            const float2 zn = zb[(N - k) & (N - 1)];
+            const float2 zk = sm[fpad(k)];
+            const float2 zn = sm[fpad((N - k) & (N - 1))];
             const float2 a = make_float2(0.5f * (zk.x + zn.x), 0.5f * (zk.y - zn.y));
             const float2 d = make_float2(zk.x - zn.x, zk.y + zn.y);
             const float2 bc = make_float2(0.5f * d.y, 0.5f * d.x);   // conj(B), B = -i d / 2
             return cmul(a, bc);
         },
-        [&](int i, float2 v, int) { corr[i] = v.x; }, sm, lt, tw);
-    // argmax over the ifftshifted correlation
-    ArgKey best;
-    best.a = -1.0f;
-    best.i = 0x7fffffff;
+        [&](int i, float2 v, int) {
+            ArgKey k;
+            k.a = fabsf(v.x);
+            k.i = (i + N / 2) & (N - 1);
+            if (argkey_better(k, best)) best = k;
+        },
+        sm, lt, tw);
+    best = block_argmax<T>(best, red);
+    if (lt == 0) s_pos = best.i;
+    __syncthreads();
+    const int pos = s_pos;
+    const int tau = (pos + N / 2) & (N - 1);
+    // f_j = sum_n a[n] b[n - (tau + j)], j = -1, 0, 1
+    float h[3] = {0.0f, 0.0f, 0.0f}, l[3] = {0.0f, 0.0f, 0.0f};
 #pragma unroll 4
     for (int t = 0; t < N / T; ++t) {
-        const int i = lt + t * T;
-        ArgKey k;
-        k.a = fabsf(corr[(i + N / 2) & (N - 1)]);
-        k.i = i;
-        if (argkey_better(k, best)) best = k;
+        const int n = lt + t * T;
+        const float a = sqrtf(ea[n]);
+#pragma unroll
+        for (int j = 0; j < 3; ++j) acc_prod(a, sqrtf(eb[(n - tau - (j - 1)) & (N - 1)]), h[j], l[j]);
     }
-    best = block_argmax<T>(best, red);
+    double f[3];
+#pragma unroll
+    for (int j = 0; j < 3; ++j) f[j] = block_sum_d<T>((double)h[j] + (double)l[j], redd);
     if (lt == 0) {
-        const int pos = best.i;
-        const float f1 = corr[((pos - 1) + N / 2) & (N - 1)];
-        const float f2 = corr[(pos + N / 2) & (N - 1)];
-        const float f3 = corr[((pos + 1) + N / 2) & (N - 1)];
-        const float fa = (f1 + f3 - 2 * f2) / 2;
-        const float fb = (f3 - f1) / 2;
-        s_res = (float)pos + (-fb / (2 * fa)) - (float)N / 2;
+        // the reference keeps the correlation in a float buffer and fits the
+        // parabola in float (binomialFixDevice, range_alignment.cu:121-131)
+        const float f1 = (float)f[0], f2 = (float)f[1], f3 = (float)f[2];
+        const float fa = __fdiv_rn(__fsub_rn(__fadd_rn(f1, f3), __fmul_rn(2.0f, f2)), 2.0f);
+        const float fb = __fdiv_rn(__fsub_rn(f3, f1), 2.0f);
+        const float delta = __fdiv_rn(-fb, __fmul_rn(2.0f, fa));
+        s_res = __fsub_rn(__fadd_rn((float)pos, delta), (float)N / 2);
     }
     __syncthreads();
     const float r = s_res;

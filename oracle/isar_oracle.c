@@ -176,15 +176,20 @@ static int argmax_abs_tree(const double* d, int cols)
     return best;
 }
 
-/* binomialFixDevice (range_alignment.cu:121-131).  Neighbours outside the
- * row wrap around (the reference reads the adjacent row there). */
-static double binomial_fix(const double* c, int pos, int n)
+/* binomialFixDevice (range_alignment.cu:121-131), in float as the reference:
+ * the correlation sits in a float buffer (d_ave_profile) and the parabola is
+ * float arithmetic.  On a broad correlation peak the second difference is
+ * tiny, so this rounding moves the shift by up to ~1e-3 cell; keeping it
+ * makes the restatement follow the reference instead of the exact value.
+ * Neighbours outside the row wrap around (the reference reads the adjacent
+ * row there). */
+static float binomial_fix(const double* c, int pos, int n)
 {
-    double f1 = c[(pos - 1 + n) % n];
-    double f2 = c[pos];
-    double f3 = c[(pos + 1) % n];
-    double fa = (f1 + f3 - 2 * f2) / 2;
-    double fb = (f3 - f1) / 2;
+    float f1 = (float)c[(pos - 1 + n) % n];
+    float f2 = (float)c[pos];
+    float f3 = (float)c[(pos + 1) % n];
+    float fa = (f1 + f3 - 2 * f2) / 2;
+    float fb = (f3 - f1) / 2;
     return -fb / (2 * fa);
 }
 
@@ -248,10 +253,9 @@ void iso_range_align(iso_cd* x, const iso_radar* p, double* shifts)
             int h2 = h1 + stride;
             correlate_shift(ave + (long)h1 * N, ave + (long)h2 * N, N, corr, tmp, tmp2);
             int pos = argmax_abs_tree(corr, N);
-            double sh = (double)pos + binomial_fix(corr, pos, N) - (double)N / 2;
-            if (shifts) shifts[shift_i] = sh;
+            float shf = (float)pos + binomial_fix(corr, pos, N) - ((float)N / 2);   /* :166 */
+            if (shifts) shifts[shift_i] = shf;
             ++shift_i;
-            float shf = (float)sh;   /* d_max_idx is a float buffer */
             for (int n = 0; n < N; ++n) {
                 iso_cd r = ramp_f32(n, shf, N);
                 for (int m = h2; m < h2 + stride; ++m) x[(long)m * N + n] *= r;
@@ -673,13 +677,17 @@ void iso_mtrc(iso_cd* cut, const iso_radar* p, int data_type)
 }
 
 /* post-processing (isar_main.cu:191-211): Hamming over pulses, column FFT,
- * column fftshift, (IFDS: flipud), |.| */
+ * column fftshift, (IFDS: flipud), |.|.
+ * The window launch (isar_main.cu:192) passes cols = echo_num and
+ * len = range_num_cut to diagMulMat(diag, data, res, cols, len)
+ * (common.cu:230-238), so it only touches the first 512 elements:
+ * element i < 512 (row 0) is scaled by hamming[i / echo_num] and every other
+ * row is left unwindowed (Q13).  Reproduced as the reference computes it. */
 void iso_post(iso_cd* cut, int M, int C, int data_type, double* img)
 {
     float* hm = (float*)malloc(sizeof(float) * M);
     iso_hamming_f32(hm, M);
-    for (int m = 0; m < M; ++m)
-        for (int c = 0; c < C; ++c) cut[(long)m * C + c] *= (double)hm[m];
+    for (int i = 0; i < ISO_RANGE_NUM_CUT && i < M * C; ++i) cut[i] *= (double)hm[i / M];
     free(hm);
     for (int c = 0; c < C; ++c) iso_fft_strided(cut + c, M, C, 0);
     shift_cols(cut, M, C);

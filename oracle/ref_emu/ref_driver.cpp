@@ -1,0 +1,64 @@
+// C entry points into the CPU-emulated reference build (TEST INFRASTRUCTURE
+// ONLY).  Compiled together with the reference's own sources; drives its
+// exported imaging path and its stage functions on host buffers.
+#include <cstring>
+#include <vector>
+
+#include "isar_imaging_export.h"
+#include "isar_main.cuh"
+
+// process globals of isar_imaging_export.cpp:4-35
+extern RadarParameters paras;
+extern CUDAHandle handles;
+extern cuComplex* d_data_proc;
+extern cuComplex* d_data_cut;
+extern double* d_velocity;
+
+extern "C" {
+
+// One frame through the reference.  echo: 2*M*N floats; velocity: M doubles.
+// img: M*512 floats (isarMainSingle).  Optional checkpoints recorded by a
+// second pass through the same stage functions in the order of
+// ISAR_RD_Imaging_Main_Ku (isar_main.cu:33-142): ra = profiles after
+// rangeAlignmentParallel (2*M*N floats), cut = after HRRPCenter + cutRangeProfile
+// and fe = after fastEntropy (2*M*512 floats each).
+int ref_frame(const float* echo, const double* velocity, int M, int N, long long band_width, long long fc,
+              double Tp, long long Fs, int data_type, int hpc, int mtrc, float* img, float* ra, float* cut,
+              float* fe)
+{
+    if (data_type != 2) return -1;
+    vec1D_FLT img_v;
+    vec1D_INT sn;
+    vec1D_DBL dn;
+    vec1D_FLT ta;
+    vec1D_COM_FLT dw;
+    const int window_len = M;
+    const int frame_len = 4 * N + 256;   // STRETCH: range_num = (frame_len - 256) / 4
+    const bool b_hpc = hpc != 0, b_hrrp = false, b_mtrc = mtrc != 0;
+    imagingMemInit(&img_v, &sn, &dn, &ta, &dw, window_len, frame_len, data_type, b_hpc, b_hrrp);
+    if (paras.echo_num != M || paras.range_num != N) return -2;
+    paras.band_width = band_width;
+    paras.fc = fc;
+    paras.Tp = Tp;
+    paras.Fs = Fs;
+    const size_t mn = (size_t)M * N;
+    std::memcpy(d_data_proc, echo, mn * sizeof(cuComplex));
+    if (b_hpc) std::memcpy(d_velocity, velocity, M * sizeof(double));
+    isarMainSingle(img, data_type, 0, 1, b_hrrp, b_hpc, b_mtrc);
+    if (ra || cut || fe) {
+        std::memcpy(d_data_proc, echo, mn * sizeof(cuComplex));
+        if (b_hpc) highSpeedCompensation(d_data_proc, d_velocity, paras, handles);
+        rangeAlignmentParallel(d_data_proc, d_hamming, paras, handles);
+        if (ra) std::memcpy(ra, d_data_proc, mn * sizeof(cuComplex));
+        HRRPCenter(d_data_proc, 30, paras, handles);
+        cutRangeProfile(d_data_proc, d_data_cut, paras.range_num, paras.range_num_cut, paras.data_num_cut,
+                        handles.handle);
+        if (cut) std::memcpy(cut, d_data_cut, (size_t)M * 512 * sizeof(cuComplex));
+        fastEntropy(d_data_cut, paras.echo_num, paras.range_num_cut, handles);
+        if (fe) std::memcpy(fe, d_data_cut, (size_t)M * 512 * sizeof(cuComplex));
+    }
+    imagingMemDest(data_type, b_hpc, b_hrrp);
+    return 0;
+}
+
+}  // extern "C"

@@ -1,0 +1,51 @@
+"""Generates the golden vectors under tests/golden/ from the reference itself.
+
+The reference's own sources (Junf137/isar_imaging_cuda/isar_imaging) are
+compiled for the CPU by oracle/ref_emu (its kernels run as host loops, Thrust
+on its CPP backend, cuFFT/cuBLAS calls on double-precision stand-ins) and
+driven through its exports (imagingMemInit + isarMainSingle) on seeded
+synthetic STRETCH frames.  Each fixture stores the int16 input, the radar
+parameters and the reference's outputs: the final image and the M x 512 cut
+after HRRPCenter + cutRangeProfile.
+
+Run here (where the reference checkout is present):
+    python tests/golden/make_golden.py
+"""
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+
+import oracle  # noqa: E402
+from oracle import ref_emu  # noqa: E402
+from tests.helpers import CFG_FULL, CFG_PLAIN, full_omega  # noqa: E402
+
+FIXTURES = {
+    # name: (M, N, full pipeline (HPC + MTRC), seed)
+    "plain_256x1024": (256, 1024, False, 101),
+    "full_256x1024": (256, 1024, True, 102),
+}
+
+
+def make(name):
+    M, N, full, seed = FIXTURES[name]
+    cfg = dict(CFG_FULL if full else CFG_PLAIN)
+    if full:
+        cfg["omega"] = full_omega(M)
+    cfg.update(M=M, N=N, seed=seed)
+    iq, vel = oracle.synth(cfg)
+    echo = oracle.iq_to_c64(iq)
+    out = ref_emu.frame(echo, vel, M, N, hpc=full, mtrc=full, checkpoints=True)
+    path = os.path.join(HERE, name + ".npz")
+    np.savez_compressed(path, iq=iq, velocity=vel, M=M, N=N, B=1e9, fc=10e9, Fs=100e6, Tp=N / 100e6,
+                        hpc=full, mtrc=full, img=out["img"], cut=out["cut"])
+    return path
+
+
+if __name__ == "__main__":
+    for n in sys.argv[1:] or FIXTURES:
+        print(make(n))

@@ -144,3 +144,23 @@ def test_full_frame(torch_cuda, gb300, M, N, full, seed):
     assert np.array_equal(tr["bins"], tw["bins"])
     assert rel_l2(got, want) < TOL_IMG
     assert abs(oracle.entropy(got) - oracle.entropy(want)) < 1e-4
+
+
+def _goldens():
+    import glob
+    import os
+    return sorted(glob.glob(os.path.join(os.path.dirname(__file__), "golden", "*.npz")))
+
+
+@pytest.mark.parametrize("path", _goldens(), ids=lambda p: p.rsplit("/", 1)[-1][:-4])
+def test_full_frame_vs_reference_golden(torch_cuda, gb300, path):
+    """The CUDA path against the reference's own outputs (tests/golden)."""
+    torch = torch_cuda
+    z = np.load(path)
+    M, N = int(z["M"]), int(z["N"])
+    flags = (gb300.FLAG_HPC if bool(z["hpc"]) else 0) | (gb300.FLAG_MTRC if bool(z["mtrc"]) else 0)
+    echo = oracle.iq_to_c64(z["iq"])
+    with ctx_for(gb300, torch, M, N) as ctx:
+        got = ctx.image_host(echo, z["velocity"], flags)
+    assert rel_l2(got, z["img"]) < TOL_IMG
+    assert abs(oracle.entropy(got) - oracle.entropy(z["img"].astype(np.float64))) < 1e-4
