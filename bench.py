@@ -204,6 +204,16 @@ def run_gb300(args):
     torch.cuda.synchronize()
     e2e_s = (time.perf_counter() - t0) / args.steps
     e2e_s = max_over_ranks(ws, e2e_s, dev)
+    # raw pinned host -> device bandwidth of one echo frame (diagnostic)
+    dst = torch.empty_like(frames[0])
+    for _ in range(3):
+        dst.copy_(hfr[0], non_blocking=True)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(5):
+        dst.copy_(hfr[0], non_blocking=True)
+    torch.cuda.synchronize()
+    h2d_gbs = 5 * hfr[0].numel() * 4 / (time.perf_counter() - t0) / 1e9
 
     out = {
         "metric": METRIC,
@@ -223,7 +233,7 @@ def run_gb300(args):
                    "120 autofocus iterations", "M": M, "N": N, "flags": "hpc+mtrc",
                    "l2": "inputs larger than L2: pool of 4 frames x 64 MiB", "parallelism": "replicas"},
         "e2e": {"value": ws / e2e_s, "unit": "frames/s", "h2d_bytes_per_step": M * N * 8 + M * 8,
-                "d2h_bytes_per_step": M * C * 4},
+                "d2h_bytes_per_step": M * C * 4, "h2d_pinned_gbs": h2d_gbs},
         "roofline": {"kernel": "range alignment (all level kernels + final transform, HPC fused)",
                      "bound": "hbm", "achieved": ra_gbs, "peak": peak, "unit": "GB/s",
                      "frac": ra_gbs / peak, "peak_kind": peak_kind, "traffic": None,

@@ -44,8 +44,12 @@ enum {
 /* DATA_TYPE (isar_imaging/common.cuh:82-87) */
 enum { ISAR_DATA_IFDS = 1, ISAR_DATA_STRETCH = 2 };
 
-/* flags for one frame: if_hpc (isar_main.cu:33), if_mtrc (isar_main.cu:160) */
-enum { ISAR_FLAG_HPC = 1, ISAR_FLAG_MTRC = 2 };
+/* flags for one frame: if_hpc (isar_main.cu:33), if_mtrc (isar_main.cu:160),
+ * if_hrrp (isar_main.cu:59).  The reference never returns the HRRP itself,
+ * but on STRETCH data getHRRP multiplies the echoes in place by the range
+ * Hamming window before range alignment (common.cu:565); ISAR_FLAG_HRRP
+ * applies that window, so the image matches the reference's with if_hrrp. */
+enum { ISAR_FLAG_HPC = 1, ISAR_FLAG_MTRC = 2, ISAR_FLAG_HRRP = 4 };
 
 /* RadarParameters (isar_imaging/common.cuh:96-117) */
 typedef struct {
@@ -112,6 +116,10 @@ ISAR_API int isar_image_host(isar_ctx* ctx, const float* echo, const double* vel
  * without HPC).  d_img: M*512 floats.
  */
 ISAR_API int isar_image_device(isar_ctx* ctx, const float* d_echo, const double* d_velocity, int flags, float* d_img);
+
+/* Waits for the context stream and reports a device-side failure of the
+ * frames queued so far (e.g. a timed-out grid barrier) as ISAR_ECUDA. */
+ISAR_API int isar_synchronize(isar_ctx* ctx);
 
 /* Device pointer of the context's M*N complex range profiles of the last
  * frame (aligned, before centering). */

@@ -19,6 +19,7 @@ STRETCH = 2
 IFDS = 1
 FLAG_HPC = 1
 FLAG_MTRC = 2
+FLAG_HRRP = 4
 RANGE_NUM_CUT = 512
 
 ISAR_OK = 0
@@ -28,7 +29,8 @@ _ERRORS = {-1: "EINVAL", -2: "ECUDA", -3: "ENOMEM", -4: "ESTATE", -5: "EIO"}
 EXPORTS = ("isar_get_last_error", "isar_version", "isar_create", "isar_destroy", "isar_stream",
            "isar_image_host", "isar_image_device", "isar_get_trace", "isar_stage_hpc",
            "isar_stage_range_align", "isar_stage_center_cut", "isar_stage_fast_entropy",
-           "isar_stage_post", "isar_fft_rows", "isar_get_profiles", "isar_synth_device", "isar_launch_count")
+           "isar_stage_post", "isar_fft_rows", "isar_get_profiles", "isar_synth_device", "isar_launch_count",
+           "isar_synchronize")
 
 
 class IsarError(RuntimeError):
@@ -93,6 +95,7 @@ def load(build_if_missing=True):
         "isar_get_profiles": (i, [vp, C.POINTER(vp)]),
         "isar_synth_device": (i, [C.POINTER(SynthParams), vp, vp, vp, vp]),
         "isar_launch_count": (C.c_longlong, []),
+        "isar_synchronize": (i, [vp]),
     }
     for name, (res, args) in sig.items():
         f = getattr(lib, name)
@@ -212,6 +215,9 @@ class Context:
     def image_device(self, d_echo, d_velocity, d_img, flags=0):
         _check(self._lib.isar_image_device(self._h, _dptr(d_echo), _dptr(d_velocity), flags, _dptr(d_img)),
                "isar_image_device")
+
+    def synchronize(self):
+        _check(self._lib.isar_synchronize(self._h), "isar_synchronize")
 
     def profiles_ptr(self):
         p = C.c_void_p()

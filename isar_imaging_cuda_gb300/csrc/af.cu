@@ -308,81 +308,118 @@ k_fe_select(const double* __restrict__ E, const double* __restrict__ H, int* __r
     if (tid < U) bins[tid] = pos[tid];
 }
 
-// gT[u][m] = cut[m][bins[u]] for u < U (transposed so that each bin is a
-// contiguous FFT input).
-__global__ void k_af_gather(const float2* __restrict__ cut, const int* __restrict__ bins,
-                            const int* __restrict__ fdec, int M, float2* __restrict__ gT)
+// Grid-wide barrier for cooperative launches (all CTAs co-resident): arrive
+// on a monotonic counter and wait, with a bounded number of polls, until it
+// reaches `target`.  A timeout sets *err and makes every later barrier fail
+// fast, so that all CTAs leave the kernel.  Returns false on failure.
+constexpr unsigned long long kSpinLimit = 1ull << 22;
+
+__device__ __forceinline__ bool grid_barrier(unsigned* count, unsigned target, int* err)
 {
-    const int U = fdec[1];
-    const int u = blockIdx.y;
-    if (u >= U) return;
-    const int b = bins[u];
-    for (int m = blockIdx.x * blockDim.x + threadIdx.x; m < M; m += gridDim.x * blockDim.x)
-        gT[(size_t)u * M + m] = cut[(size_t)m * C + b];
+    __shared__ int s_ok;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        __threadfence();
+        atomicAdd(count, 1u);
+        int ok = 1;
+        unsigned long long spins = 0;
+        for (;;) {
+            if (*(volatile unsigned*)count >= target) break;
+            if (*(volatile int*)err) {
+                ok = 0;
+                break;
+            }
+            if (++spins > kSpinLimit) {
+                atomicExch(err, 1);
+                ok = 0;
+                break;
+            }
+            __nanosleep(40);
+        }
+        __threadfence();
+        s_ok = ok;
+    }
+    __syncthreads();
+    return s_ok != 0;
 }
 
-// One minimum-entropy iteration (phase_adjustment.cu:302-318) on CB bins per
-// CTA: t = phase .* g; T = FFT(t); T .* |T|; h = IFFT(T)/M; q = conj(g) .* h;
-// per-CTA partial row sums sig_part[cta][m] = sum over the CTA's bins of q.
-template <int M, int CB>
-__global__ void __launch_bounds__(CB * M / 16)
-k_af_iter(const float2* __restrict__ gT, const float2* __restrict__ phase, const int* __restrict__ fdec,
-          float2* __restrict__ sig_part, const float2* __restrict__ tw)
+// All minimum-entropy iterations (phase_adjustment.cu:302-322) in one
+// cooperative launch of G CTAs.  CTA b owns up to 4 of the U selected bins
+// (one team of M/16 threads per bin), keeps them in shared memory, and per
+// iteration computes t = phase .* g, T = FFT(t), T .* |T|, h = IFFT(T)/M,
+// q = conj(g) .* h and writes its partial row sums to P[m][b].  After a grid
+// barrier CTA b sums the rows m = b, b+G, ... over all partials and writes
+// phase[m] = sigma / |sigma|; a second barrier publishes the new phase.
+// phase: in the Doppler-tracking start, out the final phase.
+template <int M>
+__global__ void __launch_bounds__(4 * (M / 16))
+k_af_persist(const float2* __restrict__ cut, const int* __restrict__ bins, const int* __restrict__ fdec,
+             float2* phase, float2* P, unsigned* bar, int* err, int iters, const float2* __restrict__ tw)
 {
     using F = FFTShape<M>;
+    constexpr int TEAMS = 4;
     extern __shared__ float4 dyn_smem[];
-    float2* smb = reinterpret_cast<float2*>(dyn_smem);
+    float2* gs = reinterpret_cast<float2*>(dyn_smem);   // [TEAMS][M]
+    float2* smb = gs + TEAMS * M;                        // [TEAMS][SMEM]
+    float2* ph = smb + TEAMS * F::SMEM;                  // [M]
+    const int G = gridDim.x;
     const int U = fdec[1];
-    const int u0 = blockIdx.x * CB;
-    if (u0 >= U) return;
+    const int cpc = (U + G - 1) / G;
+    const int nact = (U + cpc - 1) / cpc;                 // CTAs that own bins
     const int tid = threadIdx.x;
     const int team = tid / F::T, lt = tid % F::T;
-    const int u = u0 + team;
-    const bool valid = u < U;
-    const float2* g = gT + (size_t)u * M;
+    const int u = blockIdx.x * cpc + team;
+    const bool valid = team < cpc && u < U;
+    float2* g = gs + team * M;
     float2* sm = smb + team * F::SMEM;
-    const float invM = 1.0f / (float)M;
-    team_fft<M, false>(
-        [&](int i) { return valid ? cmul(phase[i], g[i]) : make_float2(0.0f, 0.0f); },
-        [&](int i, float2 v, int) {
-            const float a = sqrtf(v.x * v.x + v.y * v.y);
-            sm[fpad(i)] = cscale(v, a);
-        },
-        sm, lt, tw);
-    team_fft<M, true>([&](int i) { return sm[fpad(i)]; },
-                      [&](int i, float2 v, int) {
-                          const float2 h = cscale(v, invM);
-                          sm[fpad(i)] = valid ? cmulc(g[i], h) : make_float2(0.0f, 0.0f);
-                      },
-                      sm, lt, tw);
-    __syncthreads();
-    for (int m = tid; m < M; m += blockDim.x) {
-        float2 s = make_float2(0.0f, 0.0f);
-#pragma unroll
-        for (int t = 0; t < CB; ++t) {
-            const float2 q = smb[t * F::SMEM + fpad(m)];
-            s.x += q.x;
-            s.y += q.y;
-        }
-        sig_part[(size_t)blockIdx.x * M + m] = s;
+    {
+        const int b = valid ? bins[u] : 0;
+        for (int m = lt; m < M; m += F::T) g[m] = valid ? cut[(size_t)m * C + b] : make_float2(0.0f, 0.0f);
     }
-}
-
-// phase[m] = sigma[m] / |sigma[m]|, sigma = sum of the partials.
-__global__ void k_af_norm(const float2* __restrict__ sig_part, const int* __restrict__ fdec, int CB, int M,
-                          float2* __restrict__ phase)
-{
-    const int U = fdec[1];
-    const int np = (U + CB - 1) / CB;
-    for (int m = blockIdx.x * blockDim.x + threadIdx.x; m < M; m += gridDim.x * blockDim.x) {
-        float2 s = make_float2(0.0f, 0.0f);
-        for (int p = 0; p < np; ++p) {
-            const float2 q = sig_part[(size_t)p * M + m];
-            s.x += q.x;
-            s.y += q.y;
+    const float invM = 1.0f / (float)M;
+    const int lane = tid & 31, warp = tid >> 5, nwarp = blockDim.x >> 5;
+#pragma unroll 1
+    for (int it = 0; it < iters; ++it) {
+        for (int m = tid; m < M; m += blockDim.x) ph[m] = __ldcg(&phase[m]);
+        __syncthreads();
+        if (blockIdx.x < nact) {
+            team_fft<M, false>([&](int i) { return cmul(ph[i], g[i]); },
+                               [&](int i, float2 v, int) { sm[fpad(i)] = cscale(v, sqrtf(v.x * v.x + v.y * v.y)); },
+                               sm, lt, tw);
+            team_fft<M, true>([&](int i) { return sm[fpad(i)]; },
+                              [&](int i, float2 v, int) { sm[fpad(i)] = cmulc(g[i], cscale(v, invM)); }, sm, lt,
+                              tw);
+            __syncthreads();
+            for (int m = tid; m < M; m += blockDim.x) {
+                float2 s = make_float2(0.0f, 0.0f);
+#pragma unroll
+                for (int t = 0; t < TEAMS; ++t) {
+                    const float2 q = smb[t * F::SMEM + fpad(m)];
+                    s.x += q.x;
+                    s.y += q.y;
+                }
+                __stcg(&P[(size_t)m * G + blockIdx.x], s);
+            }
         }
-        const float a = sqrtf(s.x * s.x + s.y * s.y);
-        phase[m] = make_float2(s.x / a, s.y / a);
+        if (!grid_barrier(bar, (unsigned)(2 * it + 1) * G, err)) return;
+        for (int m = blockIdx.x + warp * G; m < M; m += nwarp * G) {
+            float2 s = make_float2(0.0f, 0.0f);
+            for (int b = lane; b < nact; b += 32) {
+                const float2 q = __ldcg(&P[(size_t)m * G + b]);
+                s.x += q.x;
+                s.y += q.y;
+            }
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) {
+                s.x += __shfl_xor_sync(0xffffffffu, s.x, o);
+                s.y += __shfl_xor_sync(0xffffffffu, s.y, o);
+            }
+            if (lane == 0) {
+                const float a = sqrtf(s.x * s.x + s.y * s.y);
+                __stcg(&phase[m], make_float2(s.x / a, s.y / a));
+            }
+        }
+        if (!grid_barrier(bar, (unsigned)(2 * it + 2) * G, err)) return;
     }
 }
 
@@ -406,14 +443,22 @@ static cudaError_t fe_run_m(const FEArgs& a, cudaStream_t st)
     constexpr int CB = af_cb<M>();
     using F = FFTShape<M>;
     const size_t smem = (size_t)CB * F::SMEM * sizeof(float2);
-    static bool attr = false;
-    if (!attr) {
+    const size_t smem_p = (size_t)4 * M * sizeof(float2) + (size_t)4 * F::SMEM * sizeof(float2) + M * sizeof(float2);
+    static int grid_p = 0;
+    if (grid_p == 0) {
         cudaError_t e;
         if ((e = cudaFuncSetAttribute(k_fe_colfft<M, CB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)))
             return e;
-        if ((e = cudaFuncSetAttribute(k_af_iter<M, CB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)))
+        if ((e = cudaFuncSetAttribute(k_af_persist<M>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_p)))
             return e;
-        attr = true;
+        int dev = 0, sms = 0, per_sm = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_af_persist<M>, 4 * F::T, smem_p)))
+            return e;
+        // 128 CTAs own at most 4 of the <= 512 bins each; all must be co-resident
+        grid_p = 128;
+        if (per_sm * sms < grid_p) return cudaErrorCooperativeLaunchTooLarge;
     }
     const int rows_max = M < 256 ? M : 256;
     const int R = 8;
@@ -426,17 +471,27 @@ static cudaError_t fe_run_m(const FEArgs& a, cudaStream_t st)
     ISAR_COUNT(1);
     k_fe_select<<<1, C, 0, st>>>(a.E, a.H, a.fdec, a.bins);
     ISAR_COUNT(1);
-    dim3 gg((M + 255) / 256, C);
-    k_af_gather<<<gg, 256, 0, st>>>(a.cut, a.bins, a.fdec, M, a.gT);
-    ISAR_COUNT(1);
     k_af_doppler<<<(M * 32 + 255) / 256, 256, 0, st>>>(a.cut, a.bins, a.fdec, M, a.dsum);
     ISAR_COUNT(1);
     k_fe_phase<<<1, 1024, 0, st>>>(nullptr, 0, a.dsum, M, a.phase, a.fdec);
     ISAR_COUNT(1);
-    for (int it = 0; it < a.iters; ++it) {
-        k_af_iter<M, CB><<<C / CB, CB * F::T, smem, st>>>(a.gT, a.phase, a.fdec, a.sig_part, a.tw);
-        ISAR_COUNT(1);
-        k_af_norm<<<(M + 255) / 256, 256, 0, st>>>(a.sig_part, a.fdec, CB, M, a.phase);
+    if (a.iters > 0) {
+        cudaError_t e;
+        if ((e = cudaMemsetAsync(a.bar, 0, 2 * sizeof(unsigned), st))) return e;
+        const float2* cut = a.cut;
+        const int* bins = a.bins;
+        const int* fdec = a.fdec;
+        float2* phase = a.phase;
+        float2* P = a.sig_part;
+        unsigned* bar = a.bar;
+        int* err = reinterpret_cast<int*>(a.bar + 1);
+        int iters = a.iters;
+        const float2* tw = a.tw;
+        void* args[] = {(void*)&cut, (void*)&bins, (void*)&fdec, (void*)&phase, (void*)&P,
+                        (void*)&bar, (void*)&err, (void*)&iters, (void*)&tw};
+        if ((e = cudaLaunchCooperativeKernel((const void*)k_af_persist<M>, dim3(grid_p), dim3(4 * F::T), args, smem_p,
+                                             st)))
+            return e;
         ISAR_COUNT(1);
     }
     k_af_apply<<<M, 256, 0, st>>>(a.cut, a.phase, M);

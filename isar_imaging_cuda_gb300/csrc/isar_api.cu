@@ -14,6 +14,7 @@
 #include <cstdio>
 #include <cstring>
 #include <string>
+#include <algorithm>
 #include <vector>
 
 #include "../../include/isar_gb300.h"
@@ -106,6 +107,21 @@ int next_pow2(int n)   // common.cu:521-529
     return r << 1;
 }
 
+struct FrameKey {
+    const void* x;
+    const void* vel;
+    const void* img;
+    int flags;
+    bool operator==(const FrameKey& o) const { return x == o.x && vel == o.vel && img == o.img && flags == o.flags; }
+};
+
+struct CachedGraph {
+    FrameKey key;
+    cudaGraphExec_t exec;
+    long long kernels;   // kernels per replay (for the launch counter)
+    unsigned long long tick;
+};
+
 }  // namespace
 
 struct isar_ctx {
@@ -121,6 +137,7 @@ struct isar_ctx {
     float* d_img = nullptr;
     // range alignment
     float* d_win = nullptr;
+    float* d_win_hrrp = nullptr;   // d_win * hamming (if_hrrp on STRETCH data)
     int64_t* d_hq = nullptr;
     double* d_S = nullptr;
     float* d_shifts = nullptr;
@@ -139,8 +156,8 @@ struct isar_ctx {
     double* d_E = nullptr;
     double* d_H = nullptr;
     int* d_bins = nullptr;
-    float2* d_gT = nullptr;
     float2* d_sig_part = nullptr;
+    unsigned* d_bar = nullptr;     // autofocus grid barrier: [0] counter, [1] timeout flag
     // MTRC / post
     float2* d_st = nullptr;
     float2* d_st2 = nullptr;
@@ -151,6 +168,10 @@ struct isar_ctx {
     float2* d_tw = nullptr;
     std::vector<void*> allocs;
     double hpc_coef_over_fs2 = 0.0;
+    // cached CUDA graphs of whole frames
+    bool use_graphs = true;
+    std::vector<CachedGraph> graphs;
+    unsigned long long graph_tick = 0;
 };
 
 namespace {
@@ -195,6 +216,11 @@ int build_tables(isar_ctx* c)
     hamming_f32(ham.data(), N);
     for (int n = 0; n < N; ++n) win[n] = ham[n] * (float)std::cos((double)(kPiF * (float)n));
     CU(cudaMemcpyAsync(c->d_win, win.data(), N * sizeof(float), cudaMemcpyHostToDevice, c->st));
+    // getHRRP windows the STRETCH echoes in place before range alignment
+    // (common.cu:565): x * hamming, then x * (hamming * cos(pi n))
+    std::vector<float> win_h(N);
+    for (int n = 0; n < N; ++n) win_h[n] = ham[n] * win[n];
+    CU(cudaMemcpyAsync(c->d_win_hrrp, win_h.data(), N * sizeof(float), cudaMemcpyHostToDevice, c->st));
     std::vector<float> hm(M);
     hamming_f32(hm.data(), M);
     CU(cudaMemcpyAsync(c->d_hamM, hm.data(), M * sizeof(float), cudaMemcpyHostToDevice, c->st));
@@ -246,6 +272,7 @@ int create_impl(isar_ctx* c)
     TRY(dalloc(c, &c->d_vel, M));
     TRY(dalloc(c, &c->d_img, (size_t)M * C));
     TRY(dalloc(c, &c->d_win, N));
+    TRY(dalloc(c, &c->d_win_hrrp, N));
     TRY(dalloc(c, &c->d_hq, M));
     TRY(dalloc(c, &c->d_S, M));
     TRY(dalloc(c, &c->d_shifts, M));
@@ -263,8 +290,9 @@ int create_impl(isar_ctx* c)
     TRY(dalloc(c, &c->d_E, C));
     TRY(dalloc(c, &c->d_H, C));
     TRY(dalloc(c, &c->d_bins, C));
-    TRY(dalloc(c, &c->d_gT, (size_t)C * M));
-    TRY(dalloc(c, &c->d_sig_part, (size_t)64 * M));
+    TRY(dalloc(c, &c->d_sig_part, (size_t)128 * M));
+    TRY(dalloc(c, &c->d_bar, 4));
+    CU(cudaMemsetAsync(c->d_bar, 0, 4 * sizeof(unsigned), c->st));
     TRY(dalloc(c, &c->d_st, (size_t)M * C));
     TRY(dalloc(c, &c->d_st2, (size_t)M * C));
     TRY(dalloc(c, &c->d_pre, (size_t)M * C));
@@ -277,14 +305,14 @@ int create_impl(isar_ctx* c)
     return build_tables(c);
 }
 
-isar::RAArgs ra_args(isar_ctx* c, const float2* x, float2* y, bool hpc)
+isar::RAArgs ra_args(isar_ctx* c, const float2* x, float2* y, bool hpc, bool hrrp)
 {
     isar::RAArgs a{};
     a.M = c->M;
     a.N = c->N;
     a.x = x;
     a.y = y;
-    a.win = c->d_win;
+    a.win = hrrp ? c->d_win_hrrp : c->d_win;
     a.hq = hpc ? c->d_hq : nullptr;
     a.S = c->d_S;
     a.shifts = c->d_shifts;
@@ -313,8 +341,8 @@ isar::FEArgs fe_args(isar_ctx* c, float2* cut, int iters)
     a.E = c->d_E;
     a.H = c->d_H;
     a.bins = c->d_bins;
-    a.gT = c->d_gT;
     a.sig_part = c->d_sig_part;
+    a.bar = c->d_bar;
     a.tw = c->d_tw;
     return a;
 }
@@ -344,13 +372,14 @@ int run_range_align(isar_ctx* c, const float2* x, float2* y, const double* d_vel
         if (!d_vel) return fail(ISAR_EINVAL, "ISAR_FLAG_HPC needs the pulse velocities");
         CU(isar::hpc_coef(d_vel, c->M, c->hpc_coef_over_fs2, c->d_hq, c->st));
     }
-    CU(isar::ra_run(ra_args(c, x, y, hpc), c->st));
+    const bool hrrp = (flags & ISAR_FLAG_HRRP) && c->r.data_type == ISAR_DATA_STRETCH;
+    CU(isar::ra_run(ra_args(c, x, y, hpc, hrrp), c->st));
     return ISAR_OK;
 }
 
 // x is read only, except for IFDS data whose pre-step works in place on a
 // copy in the context (d_in).
-int run_frame(isar_ctx* c, const float2* x, const double* d_vel, int flags, float* d_img)
+int run_frame_eager(isar_ctx* c, const float2* x, const double* d_vel, int flags, float* d_img)
 {
     if (c->r.data_type == ISAR_DATA_IFDS) {
         if (x != c->d_in)
@@ -362,7 +391,54 @@ int run_frame(isar_ctx* c, const float2* x, const double* d_vel, int flags, floa
     CU(isar::center_cut(c->d_arp, c->d_x, c->M, c->N, c->d_dec, c->d_cut, c->st));
     CU(isar::fe_run(fe_args(c, c->d_cut, isar::kEntropyIters), c->st));
     CU(isar::post_run(post_args(c, c->d_cut, flags, d_img), c->st));
-    c->imaged = true;
+    return ISAR_OK;
+}
+
+// One frame.  The first frame of a context runs eagerly (it also sets the
+// kernels' attributes); later frames replay a CUDA graph of the whole chain,
+// captured once per (input, velocity, image, flags) and cached (LRU of 8).
+int run_frame(isar_ctx* c, const float2* x, const double* d_vel, int flags, float* d_img)
+{
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    CU(cudaStreamIsCapturing(c->st, &cs));
+    if (!c->imaged || cs != cudaStreamCaptureStatusNone || !c->use_graphs) {
+        TRY(run_frame_eager(c, x, d_vel, flags, d_img));
+        c->imaged = true;
+        return ISAR_OK;
+    }
+    const FrameKey key{x, d_vel, d_img, flags};
+    ++c->graph_tick;
+    for (auto& g : c->graphs)
+        if (g.key == key) {
+            g.tick = c->graph_tick;
+            CU(cudaGraphLaunch(g.exec, c->st));
+            isar::launch_counter() += g.kernels;
+            return ISAR_OK;
+        }
+    const long long n0 = isar::launch_counter().load();
+    CU(cudaStreamBeginCapture(c->st, cudaStreamCaptureModeRelaxed));
+    int rc = run_frame_eager(c, x, d_vel, flags, d_img);
+    cudaGraph_t graph = nullptr;
+    cudaError_t e = cudaStreamEndCapture(c->st, &graph);
+    if (rc != ISAR_OK) {
+        if (graph) cudaGraphDestroy(graph);
+        return rc;
+    }
+    if (e != cudaSuccess) return fail(ISAR_ECUDA, "graph capture: %s", cudaGetErrorString(e));
+    CachedGraph g{key, nullptr, isar::launch_counter().load() - n0, c->graph_tick};
+    isar::launch_counter() = n0;
+    e = cudaGraphInstantiate(&g.exec, graph, 0);
+    cudaGraphDestroy(graph);
+    if (e != cudaSuccess) return fail(ISAR_ECUDA, "graph instantiate: %s", cudaGetErrorString(e));
+    if (c->graphs.size() >= 8) {
+        auto lru = std::min_element(c->graphs.begin(), c->graphs.end(),
+                                    [](const CachedGraph& a, const CachedGraph& b) { return a.tick < b.tick; });
+        cudaGraphExecDestroy(lru->exec);
+        c->graphs.erase(lru);
+    }
+    c->graphs.push_back(g);
+    CU(cudaGraphLaunch(g.exec, c->st));
+    isar::launch_counter() += g.kernels;
     return ISAR_OK;
 }
 
@@ -370,6 +446,20 @@ int check_ctx(isar_ctx* c)
 {
     if (!c) return fail(ISAR_EINVAL, "null context");
     CU(cudaSetDevice(c->dev));
+    return ISAR_OK;
+}
+
+// Waits for the context stream and reports device-side failures: the
+// autofocus kernel's grid barrier sets a flag instead of waiting forever.
+int sync_status(isar_ctx* c)
+{
+    CU(cudaStreamSynchronize(c->st));
+    unsigned flag = 0;
+    CU(cudaMemcpy(&flag, c->d_bar + 1, sizeof(unsigned), cudaMemcpyDeviceToHost));
+    if (flag) {
+        CU(cudaMemsetAsync(c->d_bar, 0, 2 * sizeof(unsigned), c->st));
+        return fail(ISAR_ECUDA, "autofocus grid barrier timed out (image of this frame is invalid)");
+    }
     return ISAR_OK;
 }
 
@@ -442,6 +532,8 @@ ISAR_API int isar_destroy(isar_ctx* c)
     if (!c) return ISAR_OK;
     cudaSetDevice(c->dev);
     if (c->st) cudaStreamSynchronize(c->st);
+    for (auto& g : c->graphs) cudaGraphExecDestroy(g.exec);
+    c->graphs.clear();
     free_all(c);
     if (c->own_stream && c->st) cudaStreamDestroy(c->st);
     delete c;
@@ -463,8 +555,13 @@ ISAR_API int isar_image_host(isar_ctx* c, const float* echo, const double* veloc
     }
     TRY(run_frame(c, c->d_in, dv, flags, c->d_img));
     CU(cudaMemcpyAsync(img, c->d_img, (size_t)c->M * kRangeCut * sizeof(float), cudaMemcpyDeviceToHost, c->st));
-    CU(cudaStreamSynchronize(c->st));
-    return ISAR_OK;
+    return sync_status(c);
+}
+
+ISAR_API int isar_synchronize(isar_ctx* c)
+{
+    TRY(check_ctx(c));
+    return sync_status(c);
 }
 
 ISAR_API int isar_image_device(isar_ctx* c, const float* d_echo, const double* d_velocity, int flags, float* d_img)
@@ -529,7 +626,7 @@ ISAR_API int isar_get_trace(isar_ctx* c, isar_trace* t)
         CU(cudaMemcpyAsync(t->ra_shift, c->d_shifts, (c->M - 1) * sizeof(float), cudaMemcpyDeviceToHost, c->st));
     if (t->phase)
         CU(cudaMemcpyAsync(t->phase, c->d_phase, c->M * sizeof(float2), cudaMemcpyDeviceToHost, c->st));
-    CU(cudaStreamSynchronize(c->st));
+    TRY(sync_status(c));
     t->center_applied = dec[0];
     t->center_shift = dec[1];
     t->cut_offset = dec[2];

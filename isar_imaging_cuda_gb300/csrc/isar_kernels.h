@@ -46,8 +46,8 @@ struct FEArgs {
     double* E;               // [512]
     double* H;               // [512]
     int* bins;               // [512]
-    float2* gT;              // [512][M]
-    float2* sig_part;        // [512/CB][M]
+    float2* sig_part;        // [M][128] autofocus partial row sums
+    unsigned* bar;           // [0] grid-barrier counter, [1] barrier timeout flag
     const float2* tw;
 };
 

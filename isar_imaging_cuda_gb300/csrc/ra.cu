@@ -202,11 +202,20 @@ __device__ float ra_correlate(float* ea, float* sm_f, int lt, const float2* __re
     return r;
 }
 
+// s + x accumulated error-free into (s, c) (TwoSum).
+__device__ __forceinline__ void two_sum_acc(float& s, float& c, float x)
+{
+    const float t = s + x;
+    const float z = t - s;
+    c += (s - (t - z)) + (x - z);
+    s = t;
+}
+
 // One row: IFFT(x * win * exp(j 2 pi (alpha n^2 - S n / N))) / N, |.|^2
-// accumulated into acc (register slots of this thread).
+// accumulated (compensated) into acc/accl (register slots of this thread).
 template <int N>
 __device__ __forceinline__ void ra_row_power(const float2* __restrict__ xr, const float* __restrict__ win,
-                                             int64_t h, int64_t sq, float* acc, float2* sm, int lt,
+                                             int64_t h, int64_t sq, float* acc, float* accl, float2* sm, int lt,
                                              const float2* __restrict__ tw)
 {
     const float invN = 1.0f / (float)N;
@@ -217,7 +226,7 @@ __device__ __forceinline__ void ra_row_power(const float2* __restrict__ xr, cons
         },
         [&](int, float2 v, int slot) {
             const float re = v.x * invN, im = v.y * invN;
-            acc[slot] += re * re + im * im;
+            two_sum_acc(acc[slot], accl[slot], re * re + im * im);
         },
         sm, lt, tw);
 }
@@ -247,23 +256,23 @@ k_ra_pair(const float2* __restrict__ x, const float* __restrict__ win, const int
         const int k = 2 * j + g;
         const int r0 = (level == 0) ? k : k * s + s / 2;
         const int nr = (level == 0) ? 1 : s / 2;
-        float acc[16];
+        float acc[16], accl[16];
 #pragma unroll
-        for (int q = 0; q < 16; ++q) acc[q] = 0.0f;
+        for (int q = 0; q < 16; ++q) acc[q] = accl[q] = 0.0f;
 #pragma unroll 1
         for (int rr = 0; rr < nr; ++rr) {
             const int row = r0 + rr;
             const int64_t h = hq ? hq[row] : 0;
             const int64_t sq = frac_to_fixed(S[row] / (double)N);
-            ra_row_power<N>(x + (size_t)row * N, win, h, sq, acc, sm, lt, tw);
+            ra_row_power<N>(x + (size_t)row * N, win, h, sq, acc, accl, sm, lt, tw);
         }
         float* e = g ? eb : ea;
 #pragma unroll
         for (int q = 0; q < 16; ++q) {
             const int i = fft_out_index<N>(lt, q);
-            float v = acc[q];
-            if (level > 0) v += left_prev[(size_t)k * lstride * N + i];
-            e[i] = v;
+            double v = (double)acc[q] + (double)accl[q];
+            if (level > 0) v += (double)left_prev[(size_t)k * lstride * N + i];
+            e[i] = (float)v;
         }
     }
     __syncthreads();
@@ -291,18 +300,18 @@ k_ra_accum(const float2* __restrict__ x, const float* __restrict__ win, const in
     const int nch = (s / 2) / rpc;
     const int k = blockIdx.x / nch, q = blockIdx.x % nch;
     const int r0 = k * s + s / 2 + q * rpc;
-    float acc[16];
+    float acc[16], accl[16];
 #pragma unroll
-    for (int t = 0; t < 16; ++t) acc[t] = 0.0f;
+    for (int t = 0; t < 16; ++t) acc[t] = accl[t] = 0.0f;
 #pragma unroll 1
     for (int rr = 0; rr < rpc; ++rr) {
         const int row = r0 + rr;
         const int64_t h = hq ? hq[row] : 0;
         const int64_t sq = frac_to_fixed(S[row] / (double)N);
-        ra_row_power<N>(x + (size_t)row * N, win, h, sq, acc, sm, lt, tw);
+        ra_row_power<N>(x + (size_t)row * N, win, h, sq, acc, accl, sm, lt, tw);
     }
 #pragma unroll
-    for (int t = 0; t < 16; ++t) part[(size_t)blockIdx.x * N + fft_out_index<N>(lt, t)] = acc[t];
+    for (int t = 0; t < 16; ++t) part[(size_t)blockIdx.x * N + fft_out_index<N>(lt, t)] = acc[t] + accl[t];
 }
 
 // E[k] = left_prev[k * lstride] + sum of the nch partials of R_k.
@@ -311,9 +320,9 @@ __global__ void k_ra_reduce(const float* __restrict__ left_prev, int lstride, co
 {
     const int k = blockIdx.y;
     for (int n = blockIdx.x * blockDim.x + threadIdx.x; n < N; n += gridDim.x * blockDim.x) {
-        float v = left_prev[(size_t)k * lstride * N + n];
-        for (int q = 0; q < nch; ++q) v += part[((size_t)k * nch + q) * N + n];
-        E[(size_t)k * N + n] = v;
+        double v = (double)left_prev[(size_t)k * lstride * N + n];
+        for (int q = 0; q < nch; ++q) v += (double)part[((size_t)k * nch + q) * N + n];
+        E[(size_t)k * N + n] = (float)v;
     }
 }
 

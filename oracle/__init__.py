@@ -17,6 +17,7 @@ STRETCH = 2
 IFDS = 1
 FLAG_HPC = 1
 FLAG_MTRC = 2
+FLAG_HRRP = 4
 
 
 class Radar(C.Structure):
@@ -99,7 +100,7 @@ def iq_to_c64(iq):
     return (iq[..., 0].astype(np.float32) + 1j * iq[..., 1].astype(np.float32)).astype(np.complex64)
 
 
-def image(echo, velocity, rp: Radar, data_type=STRETCH, hpc=False, mtrc=False, iters=120):
+def image(echo, velocity, rp: Radar, data_type=STRETCH, hpc=False, mtrc=False, iters=120, hrrp=False):
     """Runs the whole FP64 chain.  echo: complex64 [M,N].  Returns (img f64 [M,512], trace dict)."""
     M, N = rp.echo_num, rp.range_num
     e = np.ascontiguousarray(echo, np.complex64).view(np.float32).reshape(M, N, 2)
@@ -110,7 +111,7 @@ def image(echo, velocity, rp: Radar, data_type=STRETCH, hpc=False, mtrc=False, i
     tr = Trace()
     tr.ra_shift = shifts.ctypes.data_as(C.POINTER(C.c_double))
     tr.phase = phase.ctypes.data
-    flags = (FLAG_HPC if hpc else 0) | (FLAG_MTRC if mtrc else 0)
+    flags = (FLAG_HPC if hpc else 0) | (FLAG_MTRC if mtrc else 0) | (FLAG_HRRP if hrrp else 0)
     rc = lib().iso_image(_ptr(e), _ptr(v), C.byref(rp), data_type, flags, iters, _ptr(img), C.byref(tr))
     if rc != 0:
         raise ValueError("oracle rejected the frame (rc=%d)" % rc)

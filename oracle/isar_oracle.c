@@ -728,6 +728,15 @@ int iso_image(const float* echo, const double* velocity, const iso_radar* p,
         shift_rows(x, M, N);
     }
     if ((flags & ISO_FLAG_HPC) && data_type == ISO_STRETCH) iso_hpc(x, velocity, p);
+    if ((flags & ISO_FLAG_HRRP) && data_type == ISO_STRETCH) {
+        /* getHRRP (common.cu:563-566): x *= hamming(n) in place; the HRRP
+         * itself is never returned by the reference */
+        float* ham = (float*)malloc(sizeof(float) * N);
+        iso_hamming_f32(ham, N);
+        for (int m = 0; m < M; ++m)
+            for (int n = 0; n < N; ++n) x[(long)m * N + n] *= (double)ham[n];
+        free(ham);
+    }
     iso_range_align(x, p, tr ? tr->ra_shift : NULL);
     iso_hrrp_center(x, p, 30, tr);                          /* inter_length = 30 */
     int off = iso_cut(x, cut, M, N, C);

@@ -48,7 +48,8 @@ enum { ISO_IFDS = 1, ISO_STRETCH = 2 };     /* DATA_TYPE, common.cuh:82-87 */
 
 enum {
     ISO_FLAG_HPC  = 1,   /* if_hpc  (isar_main.cu:33)  */
-    ISO_FLAG_MTRC = 2    /* if_mtrc (isar_main.cu:160) */
+    ISO_FLAG_MTRC = 2,   /* if_mtrc (isar_main.cu:160) */
+    ISO_FLAG_HRRP = 4    /* if_hrrp: getHRRP windows STRETCH echoes in place (common.cu:565) */
 };
 
 #define ISO_RANGE_NUM_CUT 512           /* common.cuh:71 */
