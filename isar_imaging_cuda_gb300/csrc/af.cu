@@ -385,15 +385,15 @@ k_af_persist(const float2* __restrict__ cut, const int* __restrict__ bins, const
         if (blockIdx.x < nact) {
             team_fft<M, false>([&](int i) { return cmul(ph[i], g[i]); },
                                [&](int i, float2 v, int) { sm[fpad(i)] = cscale(v, sqrtf(v.x * v.x + v.y * v.y)); },
-                               sm, lt, tw);
+                               sm, lt, tw, valid);
             team_fft<M, true>([&](int i) { return sm[fpad(i)]; },
                               [&](int i, float2 v, int) { sm[fpad(i)] = cmulc(g[i], cscale(v, invM)); }, sm, lt,
-                              tw);
+                              tw, valid);
             __syncthreads();
+            const int nt = min(cpc, U - (int)blockIdx.x * cpc);   // bins of this CTA
             for (int m = tid; m < M; m += blockDim.x) {
                 float2 s = make_float2(0.0f, 0.0f);
-#pragma unroll
-                for (int t = 0; t < TEAMS; ++t) {
+                for (int t = 0; t < nt; ++t) {
                     const float2 q = smb[t * F::SMEM + fpad(m)];
                     s.x += q.x;
                     s.y += q.y;

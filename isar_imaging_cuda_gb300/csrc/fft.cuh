@@ -90,22 +90,29 @@ __device__ __forceinline__ void dft_reg(float2* a)
 }
 
 template <int N, int R, int NS, bool INV, bool FIRST, bool LAST, class Src, class Dst>
-__device__ __forceinline__ void fft_pass(Src& src, Dst& dst, float2* sm, int lt, const float2* __restrict__ tw)
+__device__ __forceinline__ void fft_pass(Src& src, Dst& dst, float2* sm, int lt, const float2* __restrict__ tw,
+                                         bool active)
 {
     constexpr int T = N / 16;
     constexpr int B = 16 / R;
     float2 v[16];
+    if (active) {
 #pragma unroll
-    for (int b = 0; b < B; ++b) {
-        const int j = lt + b * T;
+        for (int b = 0; b < B; ++b) {
+            const int j = lt + b * T;
 #pragma unroll
-        for (int r = 0; r < R; ++r) {
-            const int idx = j + r * (N / R);
-            if constexpr (FIRST) v[b * R + r] = src(idx);
-            else v[b * R + r] = sm[fpad(idx)];
+            for (int r = 0; r < R; ++r) {
+                const int idx = j + r * (N / R);
+                if constexpr (FIRST) v[b * R + r] = src(idx);
+                else v[b * R + r] = sm[fpad(idx)];
+            }
         }
     }
     __syncthreads();
+    if (!active) {
+        __syncthreads();
+        return;
+    }
 #pragma unroll
     for (int b = 0; b < B; ++b) {
         const int j = lt + b * T;
@@ -131,24 +138,27 @@ __device__ __forceinline__ void fft_pass(Src& src, Dst& dst, float2* sm, int lt,
 }
 
 template <int N, bool INV, int PASS, int NS, class Src, class Dst>
-__device__ __forceinline__ void fft_passes(Src& src, Dst& dst, float2* sm, int lt, const float2* __restrict__ tw)
+__device__ __forceinline__ void fft_passes(Src& src, Dst& dst, float2* sm, int lt, const float2* __restrict__ tw,
+                                           bool active)
 {
     using S = FFTShape<N>;
     constexpr int R = (PASS < S::NP16) ? 16 : (1 << S::REM);
-    fft_pass<N, R, NS, INV, PASS == 0, PASS == S::NPASS - 1>(src, dst, sm, lt, tw);
-    if constexpr (PASS + 1 < S::NPASS) fft_passes<N, INV, PASS + 1, NS * R>(src, dst, sm, lt, tw);
+    fft_pass<N, R, NS, INV, PASS == 0, PASS == S::NPASS - 1>(src, dst, sm, lt, tw, active);
+    if constexpr (PASS + 1 < S::NPASS) fft_passes<N, INV, PASS + 1, NS * R>(src, dst, sm, lt, tw, active);
 }
 
 // One team transform.  src(i) -> float2 for i in [0,N) (first pass, may read
 // global memory); dst(i, v, slot) receives output i (slot in [0,16) is the
 // register slot, fixed per thread and output index).  sm: this team's slice
 // of FFTShape<N>::SMEM float2.  lt: thread index within the team.
+// A team with active == false does no work but keeps the barriers.
 // Contains __syncthreads(): every thread of the CTA must call it.
 template <int N, bool INV, class Src, class Dst>
-__device__ __forceinline__ void team_fft(Src src, Dst dst, float2* sm, int lt, const float2* __restrict__ tw)
+__device__ __forceinline__ void team_fft(Src src, Dst dst, float2* sm, int lt, const float2* __restrict__ tw,
+                                         bool active = true)
 {
     static_assert(N >= 32 && (N & (N - 1)) == 0 && N <= kTwN, "FFT size");
-    fft_passes<N, INV, 0, 1>(src, dst, sm, lt, tw);
+    fft_passes<N, INV, 0, 1>(src, dst, sm, lt, tw, active);
 }
 
 // Output index of register slot `slot` for thread lt (the LAST pass mapping),
