@@ -167,6 +167,12 @@ typedef struct {
 ISAR_API int isar_synth_device(const isar_synth_params* p, float* d_out, double* d_velocity, double* h_velocity,
                                void* stream);
 
+/* Test hook: make range alignment use the given M-1 shifts (level-major, as
+ * isar_trace.ra_shift) instead of its own estimates; NULL restores normal
+ * operation.  Isolates the rest of the chain from the float rounding of the
+ * reference's parabolic shift estimate in parity tests. */
+ISAR_API int isar_set_ra_shifts(isar_ctx* ctx, const float* shifts);
+
 /* Batched unnormalised row FFTs of length n (512..8192) in place, for tests. */
 ISAR_API int isar_fft_rows(isar_ctx* ctx, float* d_x, int rows, int n, int inverse);
 

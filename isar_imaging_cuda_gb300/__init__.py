@@ -30,7 +30,7 @@ EXPORTS = ("isar_get_last_error", "isar_version", "isar_create", "isar_destroy",
            "isar_image_host", "isar_image_device", "isar_get_trace", "isar_stage_hpc",
            "isar_stage_range_align", "isar_stage_center_cut", "isar_stage_fast_entropy",
            "isar_stage_post", "isar_fft_rows", "isar_get_profiles", "isar_synth_device", "isar_launch_count",
-           "isar_synchronize")
+           "isar_synchronize", "isar_set_ra_shifts")
 
 
 class IsarError(RuntimeError):
@@ -96,6 +96,7 @@ def load(build_if_missing=True):
         "isar_synth_device": (i, [C.POINTER(SynthParams), vp, vp, vp, vp]),
         "isar_launch_count": (C.c_longlong, []),
         "isar_synchronize": (i, [vp]),
+        "isar_set_ra_shifts": (i, [vp, vp]),
     }
     for name, (res, args) in sig.items():
         f = getattr(lib, name)
@@ -215,6 +216,15 @@ class Context:
     def image_device(self, d_echo, d_velocity, d_img, flags=0):
         _check(self._lib.isar_image_device(self._h, _dptr(d_echo), _dptr(d_velocity), flags, _dptr(d_img)),
                "isar_image_device")
+
+    def set_ra_shifts(self, shifts=None):
+        """Test hook: range alignment uses these M-1 shifts (None: its own)."""
+        import numpy as np
+        if shifts is None:
+            _check(self._lib.isar_set_ra_shifts(self._h, None), "isar_set_ra_shifts")
+            return
+        self._given = np.ascontiguousarray(shifts, np.float32)
+        _check(self._lib.isar_set_ra_shifts(self._h, self._given.ctypes.data), "isar_set_ra_shifts")
 
     def synchronize(self):
         _check(self._lib.isar_synchronize(self._h), "isar_synchronize")

@@ -108,30 +108,30 @@ __device__ __forceinline__ void fft_pass(Src& src, Dst& dst, float2* sm, int lt,
             }
         }
     }
+    // Both barriers of a pass are executed by every thread: teams narrower than
+    // a warp share warps, so a barrier inside `if (active)` would diverge.
     __syncthreads();
-    if (!active) {
-        __syncthreads();
-        return;
-    }
+    if (active) {
 #pragma unroll
-    for (int b = 0; b < B; ++b) {
-        const int j = lt + b * T;
-        const int k = j & (NS - 1);
-        if constexpr (NS > 1) {
+        for (int b = 0; b < B; ++b) {
+            const int j = lt + b * T;
+            const int k = j & (NS - 1);
+            if constexpr (NS > 1) {
 #pragma unroll
-            for (int r = 1; r < R; ++r) {
-                float2 w = __ldg(&tw[(r * k) * (kTwN / (NS * R))]);
-                if (INV) w.y = -w.y;
-                v[b * R + r] = cmul(v[b * R + r], w);
+                for (int r = 1; r < R; ++r) {
+                    float2 w = __ldg(&tw[(r * k) * (kTwN / (NS * R))]);
+                    if (INV) w.y = -w.y;
+                    v[b * R + r] = cmul(v[b * R + r], w);
+                }
             }
-        }
-        dft_reg<R, INV>(&v[b * R]);
-        const int base = (j / NS) * NS * R + k;
+            dft_reg<R, INV>(&v[b * R]);
+            const int base = (j / NS) * NS * R + k;
 #pragma unroll
-        for (int r = 0; r < R; ++r) {
-            const int idx = base + r * NS;
-            if constexpr (LAST) dst(idx, v[b * R + r], b * R + r);
-            else sm[fpad(idx)] = v[b * R + r];
+            for (int r = 0; r < R; ++r) {
+                const int idx = base + r * NS;
+                if constexpr (LAST) dst(idx, v[b * R + r], b * R + r);
+                else sm[fpad(idx)] = v[b * R + r];
+            }
         }
     }
     __syncthreads();

@@ -168,6 +168,7 @@ struct isar_ctx {
     float2* d_tw = nullptr;
     std::vector<void*> allocs;
     double hpc_coef_over_fs2 = 0.0;
+    bool ra_given = false;         // range alignment uses injected shifts (test hook)
     // cached CUDA graphs of whole frames
     bool use_graphs = true;
     std::vector<CachedGraph> graphs;
@@ -325,6 +326,7 @@ isar::RAArgs ra_args(isar_ctx* c, const float2* x, float2* y, bool hpc, bool hrr
     a.pair_min = 128;
     a.rpc = 4;
     a.rpc_final = 4;
+    a.given_shifts = c->ra_given ? 1 : 0;
     return a;
 }
 
@@ -562,6 +564,17 @@ ISAR_API int isar_synchronize(isar_ctx* c)
 {
     TRY(check_ctx(c));
     return sync_status(c);
+}
+
+ISAR_API int isar_set_ra_shifts(isar_ctx* c, const float* shifts)
+{
+    TRY(check_ctx(c));
+    CU(cudaStreamSynchronize(c->st));
+    if (shifts) CU(cudaMemcpy(c->d_shifts, shifts, (c->M - 1) * sizeof(float), cudaMemcpyHostToDevice));
+    c->ra_given = shifts != nullptr;
+    for (auto& g : c->graphs) cudaGraphExecDestroy(g.exec);   // graphs bake the flag in
+    c->graphs.clear();
+    return ISAR_OK;
 }
 
 ISAR_API int isar_image_device(isar_ctx* c, const float* d_echo, const double* d_velocity, int flags, float* d_img)

@@ -33,6 +33,7 @@ struct RAArgs {
     int pair_min;            // use the fused pair kernel while pairs >= pair_min
     int rpc;                 // rows per CTA for the accumulate kernel
     int rpc_final;           // rows per CTA for the final transform
+    int given_shifts;        // use the shifts already in `shifts` (test hook)
 };
 
 struct FEArgs {

@@ -240,7 +240,7 @@ template <int N>
 __global__ void __launch_bounds__(N / 16)
 k_ra_pair(const float2* __restrict__ x, const float* __restrict__ win, const int64_t* __restrict__ hq,
           double* __restrict__ S, int level, const float* __restrict__ left_prev, int lstride,
-          float* __restrict__ left_next, float* __restrict__ shift_out, const float2* __restrict__ tw)
+          float* __restrict__ left_next, float* shift_out, int given, const float2* __restrict__ tw)
 {
     using F = FFTShape<N>;
     extern __shared__ float4 dyn_smem[];
@@ -279,8 +279,9 @@ k_ra_pair(const float2* __restrict__ x, const float* __restrict__ win, const int
     if (left_next)
         for (int i = lt; i < N; i += F::T) left_next[(size_t)j * N + i] = ea[i];
     __syncthreads();
-    const float sh = ra_correlate<N>(ea, sm_f, lt, tw);
-    if (lt == 0) shift_out[j] = sh;
+    const float shc = ra_correlate<N>(ea, sm_f, lt, tw);
+    const float sh = given ? shift_out[j] : shc;   // given: shifts injected by the caller (test hook)
+    if (lt == 0 && !given) shift_out[j] = sh;
     for (int m = lt; m < s; m += F::T) S[(size_t)(2 * j + 1) * s + m] += (double)sh;
 }
 
@@ -329,7 +330,7 @@ __global__ void k_ra_reduce(const float* __restrict__ left_prev, int lstride, co
 // Pair correlation on materialised envelopes E[2j], E[2j+1].
 template <int N>
 __global__ void __launch_bounds__(N / 16)
-k_ra_corr(const float* __restrict__ E, double* __restrict__ S, int level, float* __restrict__ shift_out,
+k_ra_corr(const float* __restrict__ E, double* __restrict__ S, int level, float* shift_out, int given,
           const float2* __restrict__ tw)
 {
     using F = FFTShape<N>;
@@ -341,8 +342,9 @@ k_ra_corr(const float* __restrict__ E, double* __restrict__ S, int level, float*
     const int s = 1 << level;
     for (int i = lt; i < 2 * N; i += F::T) ea[i] = E[(size_t)2 * j * N + i];
     __syncthreads();
-    const float sh = ra_correlate<N>(ea, sm_f, lt, tw);
-    if (lt == 0) shift_out[j] = sh;
+    const float shc = ra_correlate<N>(ea, sm_f, lt, tw);
+    const float sh = given ? shift_out[j] : shc;
+    if (lt == 0 && !given) shift_out[j] = sh;
     for (int m = lt; m < s; m += F::T) S[(size_t)(2 * j + 1) * s + m] += (double)sh;
 }
 
@@ -703,7 +705,7 @@ static cudaError_t ra_run_n(const RAArgs& a, cudaStream_t st)
         if (use_pair) {
             float* ln = last ? nullptr : bufs[cur];
             k_ra_pair<N><<<pairs, T, pair_smem<N>(), st>>>(a.x, a.win, a.hq, a.S, lv, left, lstride, ln,
-                                                          a.shifts + shift_off, a.tw);
+                                                          a.shifts + shift_off, a.given_shifts, a.tw);
             ISAR_COUNT(1);
             left = ln;
             lstride = 1;
@@ -718,7 +720,7 @@ static cudaError_t ra_run_n(const RAArgs& a, cudaStream_t st)
             dim3 g((N + 255) / 256, groups);
             k_ra_reduce<<<g, 256, 0, st>>>(left, lstride, a.part, nch, N, E);
             ISAR_COUNT(1);
-            k_ra_corr<N><<<pairs, T, pair_smem<N>(), st>>>(E, a.S, lv, a.shifts + shift_off, a.tw);
+            k_ra_corr<N><<<pairs, T, pair_smem<N>(), st>>>(E, a.S, lv, a.shifts + shift_off, a.given_shifts, a.tw);
             ISAR_COUNT(1);
             left = E;
             lstride = 2;
