@@ -173,6 +173,27 @@ ISAR_API int isar_synth_device(const isar_synth_params* p, float* d_out, double*
  * reference's parabolic shift estimate in parity tests. */
 ISAR_API int isar_set_ra_shifts(isar_ctx* ctx, const float* shifts);
 
+/*
+ * HRRPCenter + cutRangeProfile without a context and without allocating:
+ * the same computation as isar_stage_center_cut, profiles d_profiles
+ * (echo_num x range_num complex, device) -> d_cut (echo_num x 512 complex,
+ * device), stream-ordered on `stream` (NULL = the legacy default stream),
+ * which must belong to the calling thread's current device.  No counterpart
+ * in the reference: it is for callers that cannot allocate device memory
+ * (a fixed, pre-reserved memory budget; cudaMalloc/cudaFree, which can
+ * synchronise the device, are not allowed inside their processing loop).
+ *
+ * Scratch is one static device array per device, sized for
+ * range_num <= 8192; larger range_num returns ISAR_EINVAL.  The first call on
+ * each device sets up (symbol address and a kernel attribute, no allocation);
+ * make that first call before capturing a stream, e.g. with all arguments
+ * NULL/0, which performs the set-up only.  Calls that overlap in time on one
+ * device (different streams or threads) share the scratch and race: order
+ * them, e.g. on one stream.
+ */
+ISAR_API int isar_center_cut_noalloc(const float* d_profiles, int echo_num, int range_num, float* d_cut,
+                                     void* stream);
+
 /* Batched unnormalised row FFTs of length n (512..8192) in place, for tests. */
 ISAR_API int isar_fft_rows(isar_ctx* ctx, float* d_x, int rows, int n, int inverse);
 

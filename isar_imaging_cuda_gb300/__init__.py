@@ -30,7 +30,7 @@ EXPORTS = ("isar_get_last_error", "isar_version", "isar_create", "isar_destroy",
            "isar_image_host", "isar_image_device", "isar_get_trace", "isar_stage_hpc",
            "isar_stage_range_align", "isar_stage_center_cut", "isar_stage_fast_entropy",
            "isar_stage_post", "isar_fft_rows", "isar_get_profiles", "isar_synth_device", "isar_launch_count",
-           "isar_synchronize", "isar_set_ra_shifts")
+           "isar_synchronize", "isar_set_ra_shifts", "isar_center_cut_noalloc")
 
 
 class IsarError(RuntimeError):
@@ -97,6 +97,7 @@ def load(build_if_missing=True):
         "isar_launch_count": (C.c_longlong, []),
         "isar_synchronize": (i, [vp]),
         "isar_set_ra_shifts": (i, [vp, vp]),
+        "isar_center_cut_noalloc": (i, [vp, i, i, vp, vp]),
     }
     for name, (res, args) in sig.items():
         f = getattr(lib, name)

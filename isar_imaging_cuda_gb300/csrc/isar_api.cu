@@ -124,6 +124,8 @@ struct CachedGraph {
 
 }  // namespace
 
+int isar::record_error(int code, const char* msg) { return fail(code, "%s", msg); }
+
 struct isar_ctx {
     isar_radar r{};
     int M = 0, N = 0, dev = 0;

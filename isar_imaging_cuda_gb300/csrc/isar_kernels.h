@@ -73,6 +73,13 @@ cudaError_t ifds_pre(float2* x, int M, int N, const float2* tw, cudaStream_t st)
 cudaError_t ra_run(const RAArgs& a, cudaStream_t st);
 cudaError_t arp_from_y(const float2* y, int M, int N, float* tmp, unsigned* hmax, float* arp, cudaStream_t st);
 cudaError_t center_cut(const float* arp, const float2* y, int M, int N, int* dec, float2* cut, cudaStream_t st);
+// Raises k_center's dynamic shared-memory limit to the kMaxN case on the
+// calling thread's current device (the attribute is per device).
+cudaError_t center_prepare_current_device();
+
+// Records `msg` as the calling thread's last error (isar_get_last_error)
+// and returns `code`.
+int record_error(int code, const char* msg);
 cudaError_t fe_run(const FEArgs& a, cudaStream_t st);
 cudaError_t post_run(const PostArgs& a, cudaStream_t st);
 cudaError_t fft_rows(float2* x, int rows, int n, int inverse, const float2* tw, cudaStream_t st);

@@ -797,6 +797,11 @@ cudaError_t center_cut(const float* arp, const float2* y, int M, int N, int* dec
     return cudaGetLastError();
 }
 
+cudaError_t center_prepare_current_device()
+{
+    return cudaFuncSetAttribute(k_center, cudaFuncAttributeMaxDynamicSharedMemorySize, 2 * kMaxN * (int)sizeof(float));
+}
+
 template <int N>
 static cudaError_t ifds_n(float2* x, int M, const float2* tw, cudaStream_t st)
 {
