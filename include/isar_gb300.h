@@ -75,7 +75,27 @@ typedef struct {
     int tgt_num;              /* fastEntropy target range bins               */
     int unit2_num;            /* U, bins used by the autofocus               */
     int bins[512];            /* the U bins, ascending                       */
+    int af_iterations;        /* autofocus phase updates applied             */
+    float af_entropy;         /* entropy of the U bins at the last evaluated
+                                 phase (cluster engine; NaN otherwise)       */
 } isar_trace;
+
+/*
+ * Launch parameters of one context (no counterpart in the reference, whose
+ * parameters are compile-time constants).  Defaults reproduce the reference:
+ * 120 autofocus iterations, no stop criterion.
+ */
+typedef struct {
+    int ra_pair_min;          /* fused pair kernel while pairs >= this (128)          */
+    int ra_rows_per_cta;      /* rows per CTA of the envelope accumulation (4)        */
+    int ra_rows_final;        /* rows per CTA of the final range transform (4)        */
+    int af_cluster;           /* autofocus engine: 0 = one cooperative grid of 128    */
+                              /* CTAs; 4, 8, 16 = one thread-block cluster per frame  */
+    float af_tol;             /* stop once the entropy of the selected bins changes   */
+                              /* by <= af_tol * |entropy| (cluster engine; 0 = off)   */
+    int af_iters;             /* autofocus iterations, or the cap with af_tol (120)   */
+    int af_cluster_max;       /* out: largest af_cluster this device can launch       */
+} isar_tuning;
 
 typedef struct isar_ctx isar_ctx;
 
@@ -99,6 +119,10 @@ ISAR_API int isar_destroy(isar_ctx* ctx);
 
 /* The stream the context launches on (cudaStream_t). */
 ISAR_API void* isar_stream(isar_ctx* ctx);
+
+ISAR_API int isar_get_tuning(isar_ctx* ctx, isar_tuning* out);
+/* Validates and applies `t` (af_cluster_max is ignored); drops cached graphs. */
+ISAR_API int isar_set_tuning(isar_ctx* ctx, const isar_tuning* t);
 
 /*
  * One frame from host memory: echo = 2*M*N floats, velocity = M doubles

@@ -30,7 +30,8 @@ EXPORTS = ("isar_get_last_error", "isar_version", "isar_create", "isar_destroy",
            "isar_image_host", "isar_image_device", "isar_get_trace", "isar_stage_hpc",
            "isar_stage_range_align", "isar_stage_center_cut", "isar_stage_fast_entropy",
            "isar_stage_post", "isar_fft_rows", "isar_get_profiles", "isar_synth_device", "isar_launch_count",
-           "isar_synchronize", "isar_set_ra_shifts", "isar_center_cut_noalloc")
+           "isar_synchronize", "isar_set_ra_shifts", "isar_center_cut_noalloc", "isar_get_tuning",
+           "isar_set_tuning")
 
 
 class IsarError(RuntimeError):
@@ -55,7 +56,18 @@ class Trace(C.Structure):
     _fields_ = [("ra_shift", C.c_void_p), ("phase", C.c_void_p), ("center_applied", C.c_int),
                 ("center_shift", C.c_int), ("cut_offset", C.c_int), ("center_idx1_len", C.c_int),
                 ("center_idx2_len", C.c_int), ("center_threshold", C.c_float), ("tgt_num", C.c_int),
-                ("unit2_num", C.c_int), ("bins", C.c_int * 512)]
+                ("unit2_num", C.c_int), ("bins", C.c_int * 512), ("af_iterations", C.c_int),
+                ("af_entropy", C.c_float)]
+
+
+class Tuning(C.Structure):
+    """isar_tuning: launch parameters of a context (defaults = the reference's)."""
+    _fields_ = [("ra_pair_min", C.c_int), ("ra_rows_per_cta", C.c_int), ("ra_rows_final", C.c_int),
+                ("af_cluster", C.c_int), ("af_tol", C.c_float), ("af_iters", C.c_int),
+                ("af_cluster_max", C.c_int)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
 
 
 _lib = None
@@ -98,6 +110,8 @@ def load(build_if_missing=True):
         "isar_synchronize": (i, [vp]),
         "isar_set_ra_shifts": (i, [vp, vp]),
         "isar_center_cut_noalloc": (i, [vp, i, i, vp, vp]),
+        "isar_get_tuning": (i, [vp, C.POINTER(Tuning)]),
+        "isar_set_tuning": (i, [vp, C.POINTER(Tuning)]),
     }
     for name, (res, args) in sig.items():
         f = getattr(lib, name)
@@ -247,7 +261,23 @@ class Context:
         return dict(ra_shift=sh, phase=ph, center_applied=t.center_applied, center_shift=t.center_shift,
                     cut_offset=t.cut_offset, center_idx1_len=t.center_idx1_len,
                     center_idx2_len=t.center_idx2_len, center_threshold=t.center_threshold,
-                    tgt_num=t.tgt_num, unit2_num=U, bins=np.array(t.bins[:min(U, 512)], np.int32))
+                    tgt_num=t.tgt_num, unit2_num=U, bins=np.array(t.bins[:min(U, 512)], np.int32),
+                    af_iterations=t.af_iterations, af_entropy=t.af_entropy)
+
+    def tuning(self):
+        t = Tuning()
+        _check(self._lib.isar_get_tuning(self._h, C.byref(t)), "isar_get_tuning")
+        return t
+
+    def set_tuning(self, **kw):
+        """Updates the named isar_tuning fields, e.g. set_tuning(af_cluster=8)."""
+        t = self.tuning()
+        for k, v in kw.items():
+            if not hasattr(t, k):
+                raise KeyError(k)
+            setattr(t, k, v)
+        _check(self._lib.isar_set_tuning(self._h, C.byref(t)), "isar_set_tuning")
+        return t
 
     # stage entry points (device buffers, stream-ordered)
     def stage_hpc(self, d_x, d_vel):

@@ -1,6 +1,7 @@
 // Doppler tracking and fast minimum-entropy autofocus on the M x 512 cut.
 // Reference: phase_adjustment.cu:4-41 (dopplerTracking), :167-332
 // (fastEntropy), common.cu:341-391 (maxCols/sumCols), :436-462 (sumRows).
+#include <cooperative_groups.h>
 #include <cuda_runtime.h>
 #include <math_constants.h>
 
@@ -187,6 +188,8 @@ k_fe_colfft(const float2* __restrict__ cut, const float2* __restrict__ phase, do
     const int tid = threadIdx.x;
     const int team = tid / F::T, lt = tid % F::T;
     const int c0 = blockIdx.x * CB;
+    float2* twt = smb + CB * F::SMEM;
+    TwShared<M>::fill(twt, tw, tid, blockDim.x);
     for (int i = tid; i < M * CB; i += blockDim.x) {
         const int m = i / CB, cc = i % CB;
         smb[cc * F::SMEM + fpad(m)] = cmul(phase[m], cut[(size_t)m * C + c0 + cc]);
@@ -195,19 +198,21 @@ k_fe_colfft(const float2* __restrict__ cut, const float2* __restrict__ phase, do
     float2* sm = smb + team * F::SMEM;
     float p[16];
     team_fft<M, false>([&](int i) { return sm[fpad(i)]; },
-                       [&](int, float2 v, int slot) { p[slot] = v.x * v.x + v.y * v.y; }, sm, lt, tw);
-    double e = 0.0;
+                       [&](int, float2 v, int slot) { p[slot] = v.x * v.x + v.y * v.y; }, sm, lt,
+                       TwShared<M>{twt});
+    // per-thread partials in float (16 terms), team sums in double
+    float ep = 0.0f;
 #pragma unroll
-    for (int q = 0; q < 16; ++q) e += (double)p[q];
-    e = team_sum<F::T>(e, lt, red[team]);
+    for (int q = 0; q < 16; ++q) ep += p[q];
+    const double e = team_sum<F::T>((double)ep, lt, red[team]);
     const float ef = (float)e;
-    double h = 0.0;
+    float hp = 0.0f;
 #pragma unroll
     for (int q = 0; q < 16; ++q) {
         const float x = p[q] / ef;
-        h += (double)(-(x * logf(x)));
+        hp += -(x * logf(x));
     }
-    h = team_sum<F::T>(h, lt, red[team]);
+    const double h = team_sum<F::T>((double)hp, lt, red[team]);
     if (lt == 0) {
         E[c0 + team] = e;
         H[c0 + team] = h;
@@ -362,6 +367,9 @@ k_af_persist(const float2* __restrict__ cut, const int* __restrict__ bins, const
     float2* gs = reinterpret_cast<float2*>(dyn_smem);   // [TEAMS][M]
     float2* smb = gs + TEAMS * M;                        // [TEAMS][SMEM]
     float2* ph = smb + TEAMS * F::SMEM;                  // [M]
+    float2* twt = ph + M;                                // twiddle table
+    TwShared<M>::fill(twt, tw, threadIdx.x, blockDim.x);
+    const TwShared<M> tws{twt};
     const int G = gridDim.x;
     const int U = fdec[1];
     const int cpc = (U + G - 1) / G;
@@ -385,10 +393,10 @@ k_af_persist(const float2* __restrict__ cut, const int* __restrict__ bins, const
         if (blockIdx.x < nact) {
             team_fft<M, false>([&](int i) { return cmul(ph[i], g[i]); },
                                [&](int i, float2 v, int) { sm[fpad(i)] = cscale(v, sqrtf(v.x * v.x + v.y * v.y)); },
-                               sm, lt, tw, valid);
+                               sm, lt, tws, valid);
             team_fft<M, true>([&](int i) { return sm[fpad(i)]; },
                               [&](int i, float2 v, int) { sm[fpad(i)] = cmulc(g[i], cscale(v, invM)); }, sm, lt,
-                              tw, valid);
+                              tws, valid);
             __syncthreads();
             const int nt = min(cpc, U - (int)blockIdx.x * cpc);   // bins of this CTA
             for (int m = tid; m < M; m += blockDim.x) {
@@ -423,6 +431,197 @@ k_af_persist(const float2* __restrict__ cut, const int* __restrict__ bins, const
     }
 }
 
+// ---------------------------------------------------------------------------
+// Cluster-resident autofocus: the same iteration as k_af_persist, with all
+// state of one frame held in the shared memory of one thread-block cluster.
+//
+// CTA r of a cluster of CL owns bins [r*bpc, r*bpc + nb), bpc = ceil(U/CL),
+// processed TEAMS at a time (one team of M/16 threads per bin).  Two chunk
+// slots of TEAMS columns are cached in shared memory; a CTA owning more
+// chunks reloads the ones past the first slot from the cut every iteration.
+// Per iteration: each CTA accumulates P[m] = sum over its bins of
+// conj(g) .* IFFT(T .* |T|)/M, T = FFT(phase .* g); cluster barrier; CTA r
+// reduces rows [r*M/CL, (r+1)*M/CL) over the CL partials (distributed shared
+// memory, fixed rank order), normalises and stores the new phase into every
+// CTA's copy; cluster barrier.  The entropy of the selected bins,
+// E = ln S1 - S2/S1 with S1 = sum |T|^2, S2 = sum |T|^2 ln |T|^2, comes out of
+// the same epilogue and drives the optional stop criterion.
+// Only hardware cluster barriers: no spin-waits.
+// ---------------------------------------------------------------------------
+template <int M>
+struct AFC {
+    static constexpr int T = M / 16;
+    static constexpr int TEAMS = 4096 / M;     // 256 threads per CTA (two FFTs need ~255 registers)
+    static constexpr int THREADS = TEAMS * T;
+    static constexpr int NSLOT = 4;            // cached columns per CTA: 16384 / M
+    static constexpr size_t SMEM_F2 = 2 * (size_t)M + (size_t)TEAMS * FFTShape<M>::SMEM + (size_t)NSLOT * TEAMS * M +
+                                      TwShared<M>::kEntries;
+    static constexpr size_t SMEM = SMEM_F2 * sizeof(float2) + 64 * sizeof(double);
+};
+
+struct AFFrame {
+    const float2* cut;     // [M][512]
+    const int* bins;       // [U]
+    const int* fdec;       // [1] = U
+    float2* phase;         // [M] in: start phase, out: final phase
+    int* stat;             // [0] iterations applied, [1] entropy bits; may be null
+};
+
+template <int M>
+__global__ void __launch_bounds__(AFC<M>::THREADS, 1)
+k_af_cluster(AFFrame f, int iters, float tol, const float2* __restrict__ tw)
+{
+    namespace cg = cooperative_groups;
+    using A = AFC<M>;
+    using F = FFTShape<M>;
+    cg::cluster_group cl = cg::this_cluster();
+    const int CL = (int)cl.num_blocks();
+    const int r = (int)cl.block_rank();
+    extern __shared__ float4 dyn_smem[];
+    float2* ph = reinterpret_cast<float2*>(dyn_smem);   // [M]
+    float2* P = ph + M;                                  // [M]
+    float2* smb = P + M;                                 // [TEAMS][SMEM]
+    float2* cache = smb + A::TEAMS * F::SMEM;            // [NSLOT][TEAMS][M]
+    float2* twt = cache + (size_t)A::NSLOT * A::TEAMS * M;   // twiddle table
+    double* red = reinterpret_cast<double*>(twt + TwShared<M>::kEntries);   // [64]
+    const TwShared<M> tws{twt};
+    const int tid = threadIdx.x;
+    TwShared<M>::fill(twt, tw, tid, A::THREADS);
+    const int team = tid / F::T, lt = tid % F::T;
+    const int lane = tid & 31, warp = tid >> 5;
+    const int U = f.fdec[1];
+    const int bpc = (U + CL - 1) / CL;
+    const int b0 = r * bpc;
+    const int nb = max(0, min(bpc, U - b0));
+    const int nch = (nb + A::TEAMS - 1) / A::TEAMS;
+    const bool reload = nch > A::NSLOT;
+    float2* sm = smb + team * F::SMEM;
+
+    auto load_chunk = [&](int j, int slot) {
+        const int t = j * A::TEAMS + team;
+        float2* g = cache + ((size_t)slot * A::TEAMS + team) * M;
+        if (t < nb) {
+            const int b = f.bins[b0 + t];
+            for (int m = lt; m < M; m += F::T) g[m] = f.cut[(size_t)m * C + b];
+        }
+    };
+    for (int m = tid; m < M; m += A::THREADS) ph[m] = f.phase[m];
+    for (int j = 0; j < min(nch, A::NSLOT); ++j) load_chunk(j, j);
+    __syncthreads();
+
+    const float invM = 1.0f / (float)M;
+    const int rows = M / CL;
+    float e_prev = 0.0f;   // meaningful in thread 0
+    int used = iters;
+#pragma unroll 1
+    for (int it = 0; it < iters; ++it) {
+        for (int m = tid; m < M; m += A::THREADS) P[m] = make_float2(0.0f, 0.0f);
+        float s1 = 0.0f, s2 = 0.0f;
+#pragma unroll 1
+        for (int j = 0; j < nch; ++j) {
+            const int slot = j < A::NSLOT ? j : A::NSLOT - 1;
+            if (reload && j >= A::NSLOT - 1) {
+                __syncthreads();
+                load_chunk(j, slot);
+            }
+            __syncthreads();
+            const float2* g = cache + ((size_t)slot * A::TEAMS + team) * M;
+            const bool valid = j * A::TEAMS + team < nb;
+            team_fft<M, false>([&](int i) { return cmul(ph[i], g[i]); },
+                               [&](int i, float2 v, int) {
+                                   const float p = v.x * v.x + v.y * v.y;
+                                   s1 += p;
+                                   if (p > 0.0f) s2 += p * logf(p);
+                                   sm[fpad(i)] = cscale(v, sqrtf(p));
+                               },
+                               sm, lt, tws, valid);
+            team_fft<M, true>([&](int i) { return sm[fpad(i)]; },
+                              [&](int i, float2 v, int) { sm[fpad(i)] = cmulc(g[i], cscale(v, invM)); }, sm, lt,
+                              tws, valid);
+            const int nt = min(A::TEAMS, nb - j * A::TEAMS);
+            for (int m = tid; m < M; m += A::THREADS) {
+                float2 s = P[m];
+                for (int t = 0; t < nt; ++t) {
+                    const float2 q = smb[t * F::SMEM + fpad(m)];
+                    s.x += q.x;
+                    s.y += q.y;
+                }
+                P[m] = s;
+            }
+        }
+        // Entropy sums: float per warp, double per CTA (red[32..33]) and per
+        // cluster, all by one thread (FP64 is slow on this part).
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            s1 += __shfl_xor_sync(0xffffffffu, s1, o);
+            s2 += __shfl_xor_sync(0xffffffffu, s2, o);
+        }
+        if (lane == 0) {
+            red[warp] = s1;
+            red[16 + warp] = s2;
+        }
+        __syncthreads();
+        if (tid == 0) {
+            double a1 = 0.0, a2 = 0.0;
+            for (int w = 0; w < A::THREADS / 32; ++w) {
+                a1 += red[w];
+                a2 += red[16 + w];
+            }
+            red[32] = a1;
+            red[33] = a2;
+        }
+        cl.sync();
+        if (tid == 0) {
+            double S1 = 0.0, S2 = 0.0;
+            for (int q = 0; q < CL; ++q) {
+                const double* rr = cl.map_shared_rank(red, q);
+                S1 += rr[32];
+                S2 += rr[33];
+            }
+            const float E = logf((float)S1) - (float)S2 / (float)S1;
+            const bool stop = tol > 0.0f && it > 0 && fabsf(E - e_prev) <= tol * fabsf(E);
+            e_prev = E;
+            red[40] = stop ? 1.0 : 0.0;
+        }
+        // This CTA's rows [r*rows, (r+1)*rows) of every CTA's partial sums,
+        // gathered with independent remote loads into buf[q][row].
+        float2* buf = smb;
+        for (int idx = tid; idx < CL * rows; idx += A::THREADS) {
+            const int q = idx / rows, ml = idx - q * rows;
+            buf[idx] = cl.map_shared_rank(P, q)[r * rows + ml];
+        }
+        __syncthreads();
+        const bool stop = red[40] != 0.0;
+        if (!stop) {
+            for (int ml = tid; ml < rows; ml += A::THREADS) {
+                float2 s = make_float2(0.0f, 0.0f);
+                for (int q = 0; q < CL; ++q) {
+                    const float2 v = buf[q * rows + ml];
+                    s.x += v.x;
+                    s.y += v.y;
+                }
+                const float a = sqrtf(s.x * s.x + s.y * s.y);
+                buf[CL * rows + ml] = make_float2(s.x / a, s.y / a);
+            }
+            __syncthreads();
+            for (int idx = tid; idx < CL * rows; idx += A::THREADS) {
+                const int q = idx / rows, ml = idx - q * rows;
+                cl.map_shared_rank(ph, q)[r * rows + ml] = buf[CL * rows + ml];
+            }
+        }
+        cl.sync();
+        if (stop) {
+            used = it;
+            break;
+        }
+    }
+    for (int m = r * rows + tid; m < (r + 1) * rows; m += A::THREADS) f.phase[m] = ph[m];
+    if (r == 0 && tid == 0 && f.stat) {
+        f.stat[0] = used;
+        f.stat[1] = __float_as_int(e_prev);
+    }
+}
+
 // cut[m][c] *= phase[m]  (phase_adjustment.cu:324)
 __global__ void k_af_apply(float2* __restrict__ cut, const float2* __restrict__ phase, int M)
 {
@@ -437,13 +636,90 @@ __global__ void k_af_apply(float2* __restrict__ cut, const float2* __restrict__ 
 template <int M>
 static constexpr int af_cb() { return M >= 512 ? 8 : (M >= 256 ? 16 : 32); }
 
+// Cluster engine set-up (once per process): shared-memory limit, non-portable
+// cluster sizes, and the largest of 16/8/4 CTAs per cluster that can be
+// resident.  Returns that size, 0 if none, or a negative cudaError_t.
+template <int M>
+static int af_cluster_setup()
+{
+    static int max_cl = -1;
+    if (max_cl >= 0) return max_cl;
+    using A = AFC<M>;
+    cudaError_t e;
+    if ((e = cudaFuncSetAttribute(k_af_cluster<M>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)A::SMEM)))
+        return -(int)e;
+    if ((e = cudaFuncSetAttribute(k_af_cluster<M>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1))) {
+        (void)cudaGetLastError();
+    }
+    int best = 0;
+    for (int cl = 16; cl >= 4 && best == 0; cl >>= 1) {
+        cudaLaunchConfig_t cfg = {};
+        cudaLaunchAttribute at[1];
+        at[0].id = cudaLaunchAttributeClusterDimension;
+        at[0].val.clusterDim.x = cl;
+        at[0].val.clusterDim.y = 1;
+        at[0].val.clusterDim.z = 1;
+        cfg.gridDim = dim3(cl);
+        cfg.blockDim = dim3(A::THREADS);
+        cfg.dynamicSmemBytes = A::SMEM;
+        cfg.attrs = at;
+        cfg.numAttrs = 1;
+        int n = 0;
+        if (cudaOccupancyMaxActiveClusters(&n, k_af_cluster<M>, &cfg) == cudaSuccess && n > 0) best = cl;
+        (void)cudaGetLastError();
+    }
+    max_cl = best;
+    return max_cl;
+}
+
+template <int M>
+static cudaError_t af_cluster_launch(const FEArgs& a, cudaStream_t st)
+{
+    using A = AFC<M>;
+    const int mx = af_cluster_setup<M>();
+    if (mx < 0) return (cudaError_t)(-mx);
+    const int cl = a.af_cluster;
+    if (cl != 4 && cl != 8 && cl != 16) return cudaErrorInvalidValue;
+    if (cl > mx) return cudaErrorInvalidClusterSize;
+    cudaLaunchConfig_t cfg = {};
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeClusterDimension;
+    at[0].val.clusterDim.x = cl;
+    at[0].val.clusterDim.y = 1;
+    at[0].val.clusterDim.z = 1;
+    cfg.gridDim = dim3(cl);
+    cfg.blockDim = dim3(A::THREADS);
+    cfg.dynamicSmemBytes = A::SMEM;
+    cfg.stream = st;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    AFFrame fr{a.cut, a.bins, a.fdec, a.phase, a.af_stat};
+    cudaError_t e = cudaLaunchKernelEx(&cfg, k_af_cluster<M>, fr, a.iters, a.tol, a.tw);
+    if (e == cudaSuccess) ISAR_COUNT(1);
+    return e;
+}
+
+int af_cluster_max(int M)
+{
+    int r = 0;
+    switch (M) {
+    case 128: r = af_cluster_setup<128>(); break;
+    case 256: r = af_cluster_setup<256>(); break;
+    case 512: r = af_cluster_setup<512>(); break;
+    case 1024: r = af_cluster_setup<1024>(); break;
+    default: return 0;
+    }
+    return r < 0 ? 0 : r;
+}
+
 template <int M>
 static cudaError_t fe_run_m(const FEArgs& a, cudaStream_t st)
 {
     constexpr int CB = af_cb<M>();
     using F = FFTShape<M>;
-    const size_t smem = (size_t)CB * F::SMEM * sizeof(float2);
-    const size_t smem_p = (size_t)4 * M * sizeof(float2) + (size_t)4 * F::SMEM * sizeof(float2) + M * sizeof(float2);
+    const size_t smem = ((size_t)CB * F::SMEM + TwShared<M>::kEntries) * sizeof(float2);
+    const size_t smem_p = (size_t)4 * M * sizeof(float2) + (size_t)4 * F::SMEM * sizeof(float2) + M * sizeof(float2) +
+                          TwShared<M>::kEntries * sizeof(float2);
     static int grid_p = 0;
     if (grid_p == 0) {
         cudaError_t e;
@@ -475,7 +751,10 @@ static cudaError_t fe_run_m(const FEArgs& a, cudaStream_t st)
     ISAR_COUNT(1);
     k_fe_phase<<<1, 1024, 0, st>>>(nullptr, 0, a.dsum, M, a.phase, a.fdec);
     ISAR_COUNT(1);
-    if (a.iters > 0) {
+    if (a.iters > 0 && a.af_cluster > 0) {
+        cudaError_t e = af_cluster_launch<M>(a, st);
+        if (e) return e;
+    } else if (a.iters > 0) {
         cudaError_t e;
         if ((e = cudaMemsetAsync(a.bar, 0, 2 * sizeof(unsigned), st))) return e;
         const float2* cut = a.cut;

@@ -89,9 +89,45 @@ __device__ __forceinline__ void dft_reg(float2* a)
     }
 }
 
-template <int N, int R, int NS, bool INV, bool FIRST, bool LAST, class Src, class Dst>
-__device__ __forceinline__ void fft_pass(Src& src, Dst& dst, float2* sm, int lt, const float2* __restrict__ tw,
-                                         bool active)
+// Twiddle sources: tw(e, N) = exp(-2 pi i e / N), 0 <= e < N.
+// TwGlobal reads the global kTwN-entry table through the read-only cache.
+struct TwGlobal {
+    const float2* __restrict__ p;
+    __device__ __forceinline__ float2 operator()(int e, int n) const { return __ldg(&p[e * (kTwN / n)]); }
+};
+
+// TwShared<N>: a per-CTA shared-memory table.  For N <= 2048 it holds all N
+// twiddles; above that a two-level table hi[e >> 6] * lo[e & 63]
+// (N/64 + 64 entries, one extra complex multiply, ~1 ulp more rounding).
+template <int N>
+struct TwShared {
+    static constexpr bool kTwoLevel = N > 2048;
+    static constexpr int kEntries = kTwoLevel ? N / 64 + 64 : N;
+    const float2* p;
+    __device__ __forceinline__ float2 operator()(int e, int) const
+    {
+        if constexpr (kTwoLevel) {
+            const float2 h = p[e >> 6], l = p[N / 64 + (e & 63)];
+            return make_float2(h.x * l.x - h.y * l.y, h.x * l.y + h.y * l.x);
+        } else {
+            return p[e];
+        }
+    }
+    // Fills the table from the global kTwN table; all threads of the CTA call
+    // it, followed by a __syncthreads() before first use.
+    __device__ __forceinline__ static void fill(float2* t, const float2* __restrict__ g, int tid, int nthreads)
+    {
+        if constexpr (kTwoLevel) {
+            for (int i = tid; i < N / 64; i += nthreads) t[i] = g[(i * 64) * (kTwN / N)];
+            for (int i = tid; i < 64; i += nthreads) t[N / 64 + i] = g[i * (kTwN / N)];
+        } else {
+            for (int i = tid; i < N; i += nthreads) t[i] = g[i * (kTwN / N)];
+        }
+    }
+};
+
+template <int N, int R, int NS, bool INV, bool FIRST, bool LAST, class Src, class Dst, class Tw>
+__device__ __forceinline__ void fft_pass(Src& src, Dst& dst, float2* sm, int lt, const Tw& tw, bool active)
 {
     constexpr int T = N / 16;
     constexpr int B = 16 / R;
@@ -119,7 +155,7 @@ __device__ __forceinline__ void fft_pass(Src& src, Dst& dst, float2* sm, int lt,
             if constexpr (NS > 1) {
 #pragma unroll
                 for (int r = 1; r < R; ++r) {
-                    float2 w = __ldg(&tw[(r * k) * (kTwN / (NS * R))]);
+                    float2 w = tw((r * k) * (N / (NS * R)), N);
                     if (INV) w.y = -w.y;
                     v[b * R + r] = cmul(v[b * R + r], w);
                 }
@@ -137,9 +173,8 @@ __device__ __forceinline__ void fft_pass(Src& src, Dst& dst, float2* sm, int lt,
     __syncthreads();
 }
 
-template <int N, bool INV, int PASS, int NS, class Src, class Dst>
-__device__ __forceinline__ void fft_passes(Src& src, Dst& dst, float2* sm, int lt, const float2* __restrict__ tw,
-                                           bool active)
+template <int N, bool INV, int PASS, int NS, class Src, class Dst, class Tw>
+__device__ __forceinline__ void fft_passes(Src& src, Dst& dst, float2* sm, int lt, const Tw& tw, bool active)
 {
     using S = FFTShape<N>;
     constexpr int R = (PASS < S::NP16) ? 16 : (1 << S::REM);
@@ -153,12 +188,19 @@ __device__ __forceinline__ void fft_passes(Src& src, Dst& dst, float2* sm, int l
 // of FFTShape<N>::SMEM float2.  lt: thread index within the team.
 // A team with active == false does no work but keeps the barriers.
 // Contains __syncthreads(): every thread of the CTA must call it.
+// tw: the global kTwN table (TwGlobal) or a TwShared<N> accessor.
+template <int N, bool INV, class Src, class Dst, class Tw>
+__device__ __forceinline__ void team_fft(Src src, Dst dst, float2* sm, int lt, const Tw& tw, bool active = true)
+{
+    static_assert(N >= 32 && (N & (N - 1)) == 0 && N <= kTwN, "FFT size");
+    fft_passes<N, INV, 0, 1>(src, dst, sm, lt, tw, active);
+}
+
 template <int N, bool INV, class Src, class Dst>
 __device__ __forceinline__ void team_fft(Src src, Dst dst, float2* sm, int lt, const float2* __restrict__ tw,
                                          bool active = true)
 {
-    static_assert(N >= 32 && (N & (N - 1)) == 0 && N <= kTwN, "FFT size");
-    fft_passes<N, INV, 0, 1>(src, dst, sm, lt, tw, active);
+    team_fft<N, INV>(src, dst, sm, lt, TwGlobal{tw}, active);
 }
 
 // Output index of register slot `slot` for thread lt (the LAST pass mapping),

@@ -142,6 +142,7 @@ struct isar_ctx {
     float* d_win_hrrp = nullptr;   // d_win * hamming (if_hrrp on STRETCH data)
     int64_t* d_hq = nullptr;
     double* d_S = nullptr;
+    int64_t* d_SQ = nullptr;
     float* d_shifts = nullptr;
     float* d_env_a = nullptr;
     float* d_env_b = nullptr;
@@ -171,6 +172,13 @@ struct isar_ctx {
     std::vector<void*> allocs;
     double hpc_coef_over_fs2 = 0.0;
     bool ra_given = false;         // range alignment uses injected shifts (test hook)
+    // tuning (isar_set_tuning / the autotuner); defaults as the reference
+    int ra_pair_min = 128;
+    int ra_rpc = 4;
+    int ra_rpc_final = 4;
+    int af_cluster = 0;
+    float af_tol = 0.0f;
+    int af_iters = isar::kEntropyIters;
     // cached CUDA graphs of whole frames
     bool use_graphs = true;
     std::vector<CachedGraph> graphs;
@@ -278,6 +286,7 @@ int create_impl(isar_ctx* c)
     TRY(dalloc(c, &c->d_win_hrrp, N));
     TRY(dalloc(c, &c->d_hq, M));
     TRY(dalloc(c, &c->d_S, M));
+    TRY(dalloc(c, &c->d_SQ, M));
     TRY(dalloc(c, &c->d_shifts, M));
     TRY(dalloc(c, &c->d_env_a, (size_t)(M / 2) * N));
     TRY(dalloc(c, &c->d_env_b, (size_t)(M / 2) * N));
@@ -318,6 +327,7 @@ isar::RAArgs ra_args(isar_ctx* c, const float2* x, float2* y, bool hpc, bool hrr
     a.win = hrrp ? c->d_win_hrrp : c->d_win;
     a.hq = hpc ? c->d_hq : nullptr;
     a.S = c->d_S;
+    a.SQ = c->d_SQ;
     a.shifts = c->d_shifts;
     a.env_a = c->d_env_a;
     a.env_b = c->d_env_b;
@@ -325,9 +335,9 @@ isar::RAArgs ra_args(isar_ctx* c, const float2* x, float2* y, bool hpc, bool hrr
     a.arp = c->d_arp;
     a.hmax = c->d_hmax;
     a.tw = c->d_tw;
-    a.pair_min = 128;
-    a.rpc = 4;
-    a.rpc_final = 4;
+    a.pair_min = c->ra_pair_min;
+    a.rpc = c->ra_rpc;
+    a.rpc_final = c->ra_rpc_final;
     a.given_shifts = c->ra_given ? 1 : 0;
     return a;
 }
@@ -348,6 +358,9 @@ isar::FEArgs fe_args(isar_ctx* c, float2* cut, int iters)
     a.sig_part = c->d_sig_part;
     a.bar = c->d_bar;
     a.tw = c->d_tw;
+    a.af_cluster = c->af_cluster;
+    a.tol = c->af_tol;
+    a.af_stat = c->d_fdec + 4;
     return a;
 }
 
@@ -393,7 +406,7 @@ int run_frame_eager(isar_ctx* c, const float2* x, const double* d_vel, int flags
     }
     TRY(run_range_align(c, x, c->d_x, d_vel, flags));
     CU(isar::center_cut(c->d_arp, c->d_x, c->M, c->N, c->d_dec, c->d_cut, c->st));
-    CU(isar::fe_run(fe_args(c, c->d_cut, isar::kEntropyIters), c->st));
+    CU(isar::fe_run(fe_args(c, c->d_cut, c->af_iters), c->st));
     CU(isar::post_run(post_args(c, c->d_cut, flags, d_img), c->st));
     return ISAR_OK;
 }
@@ -651,6 +664,54 @@ ISAR_API int isar_get_trace(isar_ctx* c, isar_trace* t)
     t->tgt_num = fdec[0];
     t->unit2_num = fdec[1];
     for (int i = t->unit2_num; i < 512; ++i) t->bins[i] = 0;
+    if (c->af_cluster > 0) {
+        t->af_iterations = fdec[4];
+        std::memcpy(&t->af_entropy, &fdec[5], sizeof(float));
+    } else {
+        t->af_iterations = c->af_iters;
+        t->af_entropy = NAN;
+    }
+    return ISAR_OK;
+}
+
+ISAR_API int isar_get_tuning(isar_ctx* c, isar_tuning* t)
+{
+    TRY(check_ctx(c));
+    if (!t) return fail(ISAR_EINVAL, "null tuning");
+    t->ra_pair_min = c->ra_pair_min;
+    t->ra_rows_per_cta = c->ra_rpc;
+    t->ra_rows_final = c->ra_rpc_final;
+    t->af_cluster = c->af_cluster;
+    t->af_tol = c->af_tol;
+    t->af_iters = c->af_iters;
+    t->af_cluster_max = isar::af_cluster_max(c->M);
+    return ISAR_OK;
+}
+
+ISAR_API int isar_set_tuning(isar_ctx* c, const isar_tuning* t)
+{
+    TRY(check_ctx(c));
+    if (!t) return fail(ISAR_EINVAL, "null tuning");
+    if (t->ra_pair_min < 1 || !is_pow2(t->ra_rows_per_cta) || !is_pow2(t->ra_rows_final) || t->ra_rows_per_cta > 64 ||
+        t->ra_rows_final > 64)
+        return fail(ISAR_EINVAL, "range-alignment tuning out of range");
+    if (t->af_cluster != 0 && t->af_cluster != 4 && t->af_cluster != 8 && t->af_cluster != 16)
+        return fail(ISAR_EINVAL, "af_cluster must be 0, 4, 8 or 16");
+    if (t->af_cluster > isar::af_cluster_max(c->M))
+        return fail(ISAR_EINVAL, "af_cluster %d exceeds what this device can launch (%d)", t->af_cluster,
+                    isar::af_cluster_max(c->M));
+    if (t->af_tol < 0.0f || !(t->af_tol < 1.0f)) return fail(ISAR_EINVAL, "af_tol must be in [0, 1)");
+    if (t->af_tol > 0.0f && t->af_cluster == 0) return fail(ISAR_EINVAL, "af_tol needs the cluster engine");
+    if (t->af_iters < 0 || t->af_iters > 100000) return fail(ISAR_EINVAL, "af_iters out of range");
+    CU(cudaStreamSynchronize(c->st));
+    c->ra_pair_min = t->ra_pair_min;
+    c->ra_rpc = t->ra_rows_per_cta;
+    c->ra_rpc_final = t->ra_rows_final;
+    c->af_cluster = t->af_cluster;
+    c->af_tol = t->af_tol;
+    c->af_iters = t->af_iters;
+    for (auto& g : c->graphs) cudaGraphExecDestroy(g.exec);
+    c->graphs.clear();
     return ISAR_OK;
 }
 

@@ -23,6 +23,7 @@ struct RAArgs {
     const float* win;        // [N] hamming(n) * cos(pi*n), float as the reference
     const int64_t* hq;       // [M] HPC phase coefficient (fixed point) or nullptr
     double* S;               // [M] cumulative alignment shift, cells
+    int64_t* SQ;             // [M] S / N as a 64-bit fixed-point fraction of a cycle
     float* shifts;           // [M-1] per (level, pair) shift, level-major
     float* env_a;            // [M/2][N] envelope ping buffer
     float* env_b;            // [M/2][N] envelope pong buffer
@@ -50,7 +51,20 @@ struct FEArgs {
     float2* sig_part;        // [M][128] autofocus partial row sums
     unsigned* bar;           // [0] grid-barrier counter, [1] barrier timeout flag
     const float2* tw;
+    // Autofocus engine: 0 = one cooperative grid (128 CTAs, grid barriers);
+    // 4, 8 or 16 = one thread-block cluster of that many CTAs per frame
+    // (distributed shared memory, no grid barrier).
+    int af_cluster;
+    // Entropy stop criterion (cluster engine): stop once the entropy of the
+    // selected bins changes by <= tol * |entropy| between two iterations;
+    // 0 runs all `iters` (the reference's fixed count).
+    float tol;
+    int* af_stat;            // [0] iterations applied, [1] entropy (float bits); may be null
 };
+
+// Largest cluster the device accepts for the autofocus engine with M pulses
+// (16, 8, 4, or 0 when clusters cannot be launched).
+int af_cluster_max(int M);
 
 struct PostArgs {
     int M;

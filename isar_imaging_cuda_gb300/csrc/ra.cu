@@ -45,10 +45,23 @@ __global__ void k_hpc_coef(const double* __restrict__ vel, int M, double coef_ov
     }
 }
 
-__global__ void k_zero_d(double* __restrict__ p, int n)
+// S[m] = 0 and its fixed-point phase slope SQ[m] = 0.
+__global__ void k_zero_shift(double* __restrict__ S, int64_t* __restrict__ SQ, int n)
 {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < n) p[i] = 0.0;
+    if (i < n) {
+        S[i] = 0.0;
+        SQ[i] = 0;
+    }
+}
+
+// S[row] += sh and SQ[row] = S[row] / N as a 64-bit fixed-point fraction,
+// once per row (one thread), so that the row transforms read SQ directly.
+__device__ __forceinline__ void add_shift(double* S, int64_t* SQ, size_t row, float sh, int N)
+{
+    const double v = S[row] + (double)sh;
+    S[row] = v;
+    SQ[row] = frac_to_fixed(v / (double)N);
 }
 
 // Standalone HPC (stage test entry): x *= exp(j*2*pi*alpha_m*n^2).
@@ -108,23 +121,50 @@ __device__ __forceinline__ void acc_prod(float a, float b, float& hi, float& lo)
     hi = t;
 }
 
+// (h, l) += (h2, l2) for compensated float pairs (TwoSum on the high parts).
+__device__ __forceinline__ void pair_add(float& h, float& l, float h2, float l2)
+{
+    const float t = h + h2;
+    const float z = t - h;
+    l += l2 + ((h - (t - z)) + (h2 - z));
+    h = t;
+}
+
+// Block total of compensated float pairs as a double; valid in thread 0.
+// Float arithmetic throughout (FP64 issues slowly on this part) with the
+// precision of a double sum.
 template <int T>
-__device__ __forceinline__ double block_sum_d(double v, double* red)
+__device__ __forceinline__ double block_sum_pair0(float h, float l, float2* red)
 {
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    for (int o = 16; o > 0; o >>= 1)
+        pair_add(h, l, __shfl_xor_sync(0xffffffffu, h, o), __shfl_xor_sync(0xffffffffu, l, o));
+    double r = (double)h + (double)l;
     constexpr int W = T / 32;
     if constexpr (W > 1) {
         const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-        if (lane == 0) red[w] = v;
+        if (lane == 0) red[w] = make_float2(h, l);
         __syncthreads();
-        double t = 0.0;
-#pragma unroll
-        for (int i = 0; i < W; ++i) t += red[i];
+        if (threadIdx.x == 0) {
+            float H = red[0].x, L = red[0].y;
+            for (int i = 1; i < W; ++i) pair_add(H, L, red[i].x, red[i].y);
+            r = (double)H + (double)L;
+        }
         __syncthreads();
-        v = t;
     }
-    return v;
+    return r;
+}
+
+// float(hi + lo + x) for a compensated pair (|lo| <= ulp(hi)), rounded once
+// except in rare double-rounding ties.
+__device__ __forceinline__ float csum3(float hi, float lo, float x)
+{
+    const float s = hi + lo;
+    float e = lo - (s - hi);
+    const float t = s + x;
+    const float z = t - s;
+    e += (s - (t - z)) + (x - z);
+    return t + e;
 }
 
 // Correlates the RMS envelopes a = sqrt(ea), b = sqrt(eb) as the reference
@@ -135,15 +175,15 @@ __device__ __forceinline__ double block_sum_d(double v, double* red)
 // accumulation, because the second difference of a broad correlation peak
 // magnifies FFT rounding into ~1e-4-cell shift errors.  ea, eb are adjacent
 // N-float shared arrays and stay intact; sm_f is the FFT scratch.
-template <int N>
-__device__ float ra_correlate(float* ea, float* sm_f, int lt, const float2* __restrict__ tw)
+template <int N, class Tw>
+__device__ float ra_correlate(float* ea, float* sm_f, int lt, const Tw& tw)
 {
     using F = FFTShape<N>;
     constexpr int T = F::T;
     float2* sm = reinterpret_cast<float2*>(sm_f);
     float* eb = ea + N;
     __shared__ ArgKey red[32];
-    __shared__ double redd[32];
+    __shared__ float2 redp[32];
     __shared__ float s_res;
     __shared__ int s_pos;
     // z = a + i b, forward FFT, spectrum kept in the scratch (padded slots)
@@ -186,7 +226,7 @@ __device__ float ra_correlate(float* ea, float* sm_f, int lt, const float2* __re
     }
     double f[3];
 #pragma unroll
-    for (int j = 0; j < 3; ++j) f[j] = block_sum_d<T>((double)h[j] + (double)l[j], redd);
+    for (int j = 0; j < 3; ++j) f[j] = block_sum_pair0<T>(h[j], l[j], redp);
     if (lt == 0) {
         // the reference keeps the correlation in a float buffer and fits the
         // parabola in float (binomialFixDevice, range_alignment.cu:121-131)
@@ -213,10 +253,10 @@ __device__ __forceinline__ void two_sum_acc(float& s, float& c, float x)
 
 // One row: IFFT(x * win * exp(j 2 pi (alpha n^2 - S n / N))) / N, |.|^2
 // accumulated (compensated) into acc/accl (register slots of this thread).
-template <int N>
+template <int N, class Tw>
 __device__ __forceinline__ void ra_row_power(const float2* __restrict__ xr, const float* __restrict__ win,
                                              int64_t h, int64_t sq, float* acc, float* accl, float2* sm, int lt,
-                                             const float2* __restrict__ tw)
+                                             const Tw& tw)
 {
     const float invN = 1.0f / (float)N;
     team_fft<N, true>(
@@ -239,8 +279,8 @@ __device__ __forceinline__ void ra_row_power(const float2* __restrict__ xr, cons
 template <int N>
 __global__ void __launch_bounds__(N / 16)
 k_ra_pair(const float2* __restrict__ x, const float* __restrict__ win, const int64_t* __restrict__ hq,
-          double* __restrict__ S, int level, const float* __restrict__ left_prev, int lstride,
-          float* __restrict__ left_next, float* shift_out, int given, const float2* __restrict__ tw)
+          double* __restrict__ S, int64_t* __restrict__ SQ, int level, const float* __restrict__ left_prev,
+          int lstride, float* __restrict__ left_next, float* shift_out, int given, const float2* __restrict__ tw)
 {
     using F = FFTShape<N>;
     extern __shared__ float4 dyn_smem[];
@@ -251,6 +291,10 @@ k_ra_pair(const float2* __restrict__ x, const float* __restrict__ win, const int
     const int s = 1 << level;
     const int j = blockIdx.x;
     float2* sm = reinterpret_cast<float2*>(sm_f);
+    float2* twt = reinterpret_cast<float2*>(eb + N);
+    TwShared<N>::fill(twt, tw, lt, F::T);
+    __syncthreads();
+    const TwShared<N> tws{twt};
 #pragma unroll 1
     for (int g = 0; g < 2; ++g) {
         const int k = 2 * j + g;
@@ -263,26 +307,24 @@ k_ra_pair(const float2* __restrict__ x, const float* __restrict__ win, const int
         for (int rr = 0; rr < nr; ++rr) {
             const int row = r0 + rr;
             const int64_t h = hq ? hq[row] : 0;
-            const int64_t sq = frac_to_fixed(S[row] / (double)N);
-            ra_row_power<N>(x + (size_t)row * N, win, h, sq, acc, accl, sm, lt, tw);
+            ra_row_power<N>(x + (size_t)row * N, win, h, SQ[row], acc, accl, sm, lt, tws);
         }
         float* e = g ? eb : ea;
 #pragma unroll
         for (int q = 0; q < 16; ++q) {
             const int i = fft_out_index<N>(lt, q);
-            double v = (double)acc[q] + (double)accl[q];
-            if (level > 0) v += (double)left_prev[(size_t)k * lstride * N + i];
-            e[i] = (float)v;
+            const float lp = (level > 0) ? left_prev[(size_t)k * lstride * N + i] : 0.0f;
+            e[i] = csum3(acc[q], accl[q], lp);
         }
     }
     __syncthreads();
     if (left_next)
         for (int i = lt; i < N; i += F::T) left_next[(size_t)j * N + i] = ea[i];
     __syncthreads();
-    const float shc = ra_correlate<N>(ea, sm_f, lt, tw);
+    const float shc = ra_correlate<N>(ea, sm_f, lt, tws);
     const float sh = given ? shift_out[j] : shc;   // given: shifts injected by the caller (test hook)
     if (lt == 0 && !given) shift_out[j] = sh;
-    for (int m = lt; m < s; m += F::T) S[(size_t)(2 * j + 1) * s + m] += (double)sh;
+    for (int m = lt; m < s; m += F::T) add_shift(S, SQ, (size_t)(2 * j + 1) * s + m, sh, N);
 }
 
 // Level >= 1, many rows per group: CTA b transforms rpc rows of R_k
@@ -290,7 +332,7 @@ k_ra_pair(const float2* __restrict__ x, const float* __restrict__ win, const int
 template <int N>
 __global__ void __launch_bounds__(N / 16)
 k_ra_accum(const float2* __restrict__ x, const float* __restrict__ win, const int64_t* __restrict__ hq,
-           const double* __restrict__ S, int level, int rpc, float* __restrict__ part,
+           const int64_t* __restrict__ SQ, int level, int rpc, float* __restrict__ part,
            const float2* __restrict__ tw)
 {
     using F = FFTShape<N>;
@@ -301,6 +343,10 @@ k_ra_accum(const float2* __restrict__ x, const float* __restrict__ win, const in
     const int nch = (s / 2) / rpc;
     const int k = blockIdx.x / nch, q = blockIdx.x % nch;
     const int r0 = k * s + s / 2 + q * rpc;
+    float2* twt = sm + F::SMEM;
+    TwShared<N>::fill(twt, tw, lt, F::T);
+    __syncthreads();
+    const TwShared<N> tws{twt};
     float acc[16], accl[16];
 #pragma unroll
     for (int t = 0; t < 16; ++t) acc[t] = accl[t] = 0.0f;
@@ -308,30 +354,30 @@ k_ra_accum(const float2* __restrict__ x, const float* __restrict__ win, const in
     for (int rr = 0; rr < rpc; ++rr) {
         const int row = r0 + rr;
         const int64_t h = hq ? hq[row] : 0;
-        const int64_t sq = frac_to_fixed(S[row] / (double)N);
-        ra_row_power<N>(x + (size_t)row * N, win, h, sq, acc, accl, sm, lt, tw);
+        ra_row_power<N>(x + (size_t)row * N, win, h, SQ[row], acc, accl, sm, lt, tws);
     }
 #pragma unroll
     for (int t = 0; t < 16; ++t) part[(size_t)blockIdx.x * N + fft_out_index<N>(lt, t)] = acc[t] + accl[t];
 }
 
-// E[k] = left_prev[k * lstride] + sum of the nch partials of R_k.
+// E[k] = left_prev[k * lstride] + sum of the nch partials of R_k
+// (compensated float sum).
 __global__ void k_ra_reduce(const float* __restrict__ left_prev, int lstride, const float* __restrict__ part,
                             int nch, int N, float* __restrict__ E)
 {
     const int k = blockIdx.y;
     for (int n = blockIdx.x * blockDim.x + threadIdx.x; n < N; n += gridDim.x * blockDim.x) {
-        double v = (double)left_prev[(size_t)k * lstride * N + n];
-        for (int q = 0; q < nch; ++q) v += (double)part[((size_t)k * nch + q) * N + n];
-        E[(size_t)k * N + n] = (float)v;
+        float h = left_prev[(size_t)k * lstride * N + n], l = 0.0f;
+        for (int q = 0; q < nch; ++q) two_sum_acc(h, l, part[((size_t)k * nch + q) * N + n]);
+        E[(size_t)k * N + n] = h + l;
     }
 }
 
 // Pair correlation on materialised envelopes E[2j], E[2j+1].
 template <int N>
 __global__ void __launch_bounds__(N / 16)
-k_ra_corr(const float* __restrict__ E, double* __restrict__ S, int level, float* shift_out, int given,
-          const float2* __restrict__ tw)
+k_ra_corr(const float* __restrict__ E, double* __restrict__ S, int64_t* __restrict__ SQ, int level,
+          float* shift_out, int given, const float2* __restrict__ tw)
 {
     using F = FFTShape<N>;
     extern __shared__ float4 dyn_smem[];
@@ -340,12 +386,14 @@ k_ra_corr(const float* __restrict__ E, double* __restrict__ S, int level, float*
     const int lt = threadIdx.x;
     const int j = blockIdx.x;
     const int s = 1 << level;
+    float2* twt = reinterpret_cast<float2*>(ea + 2 * N);
+    TwShared<N>::fill(twt, tw, lt, F::T);
     for (int i = lt; i < 2 * N; i += F::T) ea[i] = E[(size_t)2 * j * N + i];
     __syncthreads();
-    const float shc = ra_correlate<N>(ea, sm_f, lt, tw);
+    const float shc = ra_correlate<N>(ea, sm_f, lt, TwShared<N>{twt});
     const float sh = given ? shift_out[j] : shc;
     if (lt == 0 && !given) shift_out[j] = sh;
-    for (int m = lt; m < s; m += F::T) S[(size_t)(2 * j + 1) * s + m] += (double)sh;
+    for (int m = lt; m < s; m += F::T) add_shift(S, SQ, (size_t)(2 * j + 1) * s + m, sh, N);
 }
 
 // Final transform of all rows, written in place: y = IFFT(x*win*ramp)/N.
@@ -354,7 +402,7 @@ k_ra_corr(const float* __restrict__ E, double* __restrict__ S, int level, float*
 template <int N>
 __global__ void __launch_bounds__(N / 16)
 k_ra_final(const float2* x, float2* yout, const float* __restrict__ win, const int64_t* __restrict__ hq,
-           const double* __restrict__ S, int rpc, int arp_rows, float* __restrict__ arp_part,
+           const int64_t* __restrict__ SQ, int rpc, int arp_rows, float* __restrict__ arp_part,
            unsigned* __restrict__ hmax, const float2* __restrict__ tw)
 {
     using F = FFTShape<N>;
@@ -364,6 +412,10 @@ k_ra_final(const float2* x, float2* yout, const float* __restrict__ win, const i
     const int lt = threadIdx.x;
     const int r0 = blockIdx.x * rpc;
     const float invN = 1.0f / (float)N;
+    float2* twt = sm + F::SMEM;
+    TwShared<N>::fill(twt, tw, lt, F::T);
+    __syncthreads();
+    const TwShared<N> tws{twt};
     float acc[16];
 #pragma unroll
     for (int t = 0; t < 16; ++t) acc[t] = 0.0f;
@@ -372,7 +424,7 @@ k_ra_final(const float2* x, float2* yout, const float* __restrict__ win, const i
     for (int rr = 0; rr < rpc; ++rr) {
         const int row = r0 + rr;
         const int64_t h = hq ? hq[row] : 0;
-        const int64_t sq = frac_to_fixed(S[row] / (double)N);
+        const int64_t sq = SQ[row];
         const float2* xr = x + (size_t)row * N;
         float2* yr = yout + (size_t)row * N;
         const bool arp = row < arp_rows;
@@ -385,7 +437,7 @@ k_ra_final(const float2* x, float2* yout, const float* __restrict__ win, const i
                 mx = fmaxf(mx, a);
                 if (arp) acc[slot] += a;
             },
-            sm, lt, tw);
+            sm, lt, tws);
     }
     if (r0 < arp_rows) {
 #pragma unroll
@@ -658,9 +710,12 @@ __global__ void __launch_bounds__(N / 16) k_fft_rows(float2* x, const float2* __
 // host launchers
 // ---------------------------------------------------------------------------
 template <int N>
-static size_t pair_smem() { return (size_t)FFTShape<N>::SMEM * sizeof(float2) + 2 * N * sizeof(float); }
+static size_t pair_smem()
+{
+    return ((size_t)FFTShape<N>::SMEM + TwShared<N>::kEntries) * sizeof(float2) + 2 * N * sizeof(float);
+}
 template <int N>
-static size_t fft_smem() { return (size_t)FFTShape<N>::SMEM * sizeof(float2); }
+static size_t fft_smem() { return ((size_t)FFTShape<N>::SMEM + TwShared<N>::kEntries) * sizeof(float2); }
 
 template <int N>
 static cudaError_t set_attrs()
@@ -690,7 +745,7 @@ static cudaError_t ra_run_n(const RAArgs& a, cudaStream_t st)
     const int T = N / 16;
     int L = 0;
     while ((1 << L) < M) ++L;
-    k_zero_d<<<(M + 255) / 256, 256, 0, st>>>(a.S, M);
+    k_zero_shift<<<(M + 255) / 256, 256, 0, st>>>(a.S, a.SQ, M);
     ISAR_COUNT(1);
     const float* left = nullptr;
     int lstride = 1;
@@ -704,7 +759,7 @@ static cudaError_t ra_run_n(const RAArgs& a, cudaStream_t st)
         const bool use_pair = (lv == 0) || pairs >= a.pair_min || (s / 2) <= 1;
         if (use_pair) {
             float* ln = last ? nullptr : bufs[cur];
-            k_ra_pair<N><<<pairs, T, pair_smem<N>(), st>>>(a.x, a.win, a.hq, a.S, lv, left, lstride, ln,
+            k_ra_pair<N><<<pairs, T, pair_smem<N>(), st>>>(a.x, a.win, a.hq, a.S, a.SQ, lv, left, lstride, ln,
                                                           a.shifts + shift_off, a.given_shifts, a.tw);
             ISAR_COUNT(1);
             left = ln;
@@ -714,13 +769,14 @@ static cudaError_t ra_run_n(const RAArgs& a, cudaStream_t st)
             if (rpc > s / 2) rpc = s / 2;
             const int nch = (s / 2) / rpc;
             const int groups = M / s;
-            k_ra_accum<N><<<groups * nch, T, fft_smem<N>(), st>>>(a.x, a.win, a.hq, a.S, lv, rpc, a.part, a.tw);
+            k_ra_accum<N><<<groups * nch, T, fft_smem<N>(), st>>>(a.x, a.win, a.hq, a.SQ, lv, rpc, a.part, a.tw);
             ISAR_COUNT(1);
             float* E = bufs[cur];
             dim3 g((N + 255) / 256, groups);
             k_ra_reduce<<<g, 256, 0, st>>>(left, lstride, a.part, nch, N, E);
             ISAR_COUNT(1);
-            k_ra_corr<N><<<pairs, T, pair_smem<N>(), st>>>(E, a.S, lv, a.shifts + shift_off, a.given_shifts, a.tw);
+            k_ra_corr<N><<<pairs, T, pair_smem<N>(), st>>>(E, a.S, a.SQ, lv, a.shifts + shift_off, a.given_shifts,
+                                                          a.tw);
             ISAR_COUNT(1);
             left = E;
             lstride = 2;
@@ -734,7 +790,8 @@ static cudaError_t ra_run_n(const RAArgs& a, cudaStream_t st)
     const int arp_rows = M < 256 ? M : 256;
     int rpcf = a.rpc_final;
     while (rpcf > 1 && (M % rpcf)) rpcf >>= 1;
-    k_ra_final<N><<<M / rpcf, T, fft_smem<N>(), st>>>(a.x, a.y, a.win, a.hq, a.S, rpcf, arp_rows, a.part, a.hmax, a.tw);
+    k_ra_final<N><<<M / rpcf, T, fft_smem<N>(), st>>>(a.x, a.y, a.win, a.hq, a.SQ, rpcf, arp_rows, a.part, a.hmax,
+                                                      a.tw);
     ISAR_COUNT(1);
     const int nparts = (arp_rows + rpcf - 1) / rpcf;
     k_arp_reduce<<<(N + 255) / 256, 256, 0, st>>>(a.part, nparts, N, M, a.hmax, a.arp);
