@@ -218,6 +218,48 @@ ISAR_API int isar_set_ra_shifts(isar_ctx* ctx, const float* shifts);
 ISAR_API int isar_center_cut_noalloc(const float* d_profiles, int echo_num, int range_num, float* d_cut,
                                      void* stream);
 
+/*
+ * Autotuner (no counterpart in the reference): times whole frames of
+ * d_echo on this context over the range-alignment knobs and the autofocus
+ * engines allowed by `engines` (bit 0: cooperative grid, bit 1: clusters),
+ * coordinate by coordinate, applies the fastest and returns it.  Keeps
+ * af_tol and af_iters.  Blocking; allocates a scratch image while it runs.
+ */
+ISAR_API int isar_autotune(isar_ctx* ctx, const float* d_echo, const double* d_velocity, int flags, int engines,
+                           isar_tuning* out);
+
+/* ---- batches: many frames of uneven size in one CUDA graph ---------------
+ * No counterpart in the reference (one frame per isarMainSingle).  Frames are
+ * grouped by isar_radar; each group is dealt round-robin to `lanes` contexts
+ * with their own streams; the whole batch is captured once into a CUDA graph
+ * (fork/join on the batch stream) and replayed.  Lanes use the cluster
+ * autofocus engine.  Results equal those of isar_image_device with the same
+ * isar_tuning. */
+typedef struct {
+    isar_radar radar;         /* M, N and radar parameters of this frame         */
+    const float* d_echo;      /* device, 2*M*N floats, read only                 */
+    const double* d_velocity; /* device, M doubles (ISAR_FLAG_HPC), or NULL      */
+    int flags;                /* ISAR_FLAG_*                                     */
+    float* d_img;             /* device, M*512 floats                            */
+} isar_batch_frame;
+
+typedef struct isar_batch isar_batch;
+
+/* lanes: contexts per frame shape (0 = 4); `stream` = cudaStream_t or NULL. */
+ISAR_API int isar_batch_create(isar_batch** out, int device, void* stream, int lanes);
+ISAR_API int isar_batch_destroy(isar_batch* b);
+ISAR_API void* isar_batch_stream(isar_batch* b);
+/* Stream-ordered on isar_batch_stream(b); the graph is cached per frame list. */
+ISAR_API int isar_batch_run(isar_batch* b, const isar_batch_frame* frames, int n);
+/* Waits for the batch and reports device-side failures. */
+ISAR_API int isar_batch_synchronize(isar_batch* b);
+ISAR_API int isar_batch_set_tuning(isar_batch* b, const isar_radar* shape, const isar_tuning* t);
+ISAR_API int isar_batch_get_tuning(isar_batch* b, const isar_radar* shape, isar_tuning* out);
+ISAR_API int isar_batch_lanes(isar_batch* b);
+/* Tunes each shape (isar_autotune, cluster engine) and the lanes per shape
+ * on this frame list; *best_ms (may be NULL) = the fastest batch time. */
+ISAR_API int isar_batch_autotune(isar_batch* b, const isar_batch_frame* frames, int n, float* best_ms);
+
 /* Batched unnormalised row FFTs of length n (512..8192) in place, for tests. */
 ISAR_API int isar_fft_rows(isar_ctx* ctx, float* d_x, int rows, int n, int inverse);
 

@@ -31,7 +31,9 @@ EXPORTS = ("isar_get_last_error", "isar_version", "isar_create", "isar_destroy",
            "isar_stage_range_align", "isar_stage_center_cut", "isar_stage_fast_entropy",
            "isar_stage_post", "isar_fft_rows", "isar_get_profiles", "isar_synth_device", "isar_launch_count",
            "isar_synchronize", "isar_set_ra_shifts", "isar_center_cut_noalloc", "isar_get_tuning",
-           "isar_set_tuning")
+           "isar_set_tuning", "isar_autotune", "isar_batch_create", "isar_batch_destroy", "isar_batch_stream",
+           "isar_batch_run", "isar_batch_synchronize", "isar_batch_set_tuning", "isar_batch_get_tuning",
+           "isar_batch_lanes", "isar_batch_autotune")
 
 
 class IsarError(RuntimeError):
@@ -112,6 +114,16 @@ def load(build_if_missing=True):
         "isar_center_cut_noalloc": (i, [vp, i, i, vp, vp]),
         "isar_get_tuning": (i, [vp, C.POINTER(Tuning)]),
         "isar_set_tuning": (i, [vp, C.POINTER(Tuning)]),
+        "isar_autotune": (i, [vp, vp, vp, i, i, C.POINTER(Tuning)]),
+        "isar_batch_create": (i, [C.POINTER(vp), i, vp, i]),
+        "isar_batch_destroy": (i, [vp]),
+        "isar_batch_stream": (vp, [vp]),
+        "isar_batch_run": (i, [vp, vp, i]),
+        "isar_batch_synchronize": (i, [vp]),
+        "isar_batch_set_tuning": (i, [vp, C.POINTER(Radar), C.POINTER(Tuning)]),
+        "isar_batch_get_tuning": (i, [vp, C.POINTER(Radar), C.POINTER(Tuning)]),
+        "isar_batch_lanes": (i, [vp]),
+        "isar_batch_autotune": (i, [vp, vp, i, C.POINTER(C.c_float)]),
     }
     for name, (res, args) in sig.items():
         f = getattr(lib, name)
@@ -298,3 +310,80 @@ class Context:
 
     def fft_rows(self, d_x, rows, n, inverse=False):
         _check(self._lib.isar_fft_rows(self._h, _dptr(d_x), rows, n, 1 if inverse else 0), "isar_fft_rows")
+
+    def autotune(self, d_echo, d_velocity=None, flags=0, engines=3):
+        """isar_autotune: times frames of d_echo over the launch parameters,
+        applies and returns the fastest isar_tuning."""
+        t = Tuning()
+        _check(self._lib.isar_autotune(self._h, _dptr(d_echo), _dptr(d_velocity), flags, engines, C.byref(t)),
+               "isar_autotune")
+        return t
+
+
+class BatchFrame(C.Structure):
+    """isar_batch_frame: one frame of a batch (device buffers)."""
+    _fields_ = [("radar", Radar), ("d_echo", C.c_void_p), ("d_velocity", C.c_void_p), ("flags", C.c_int),
+                ("d_img", C.c_void_p)]
+
+
+class Batch:
+    """Many frames of uneven size imaged by one CUDA graph (isar_batch_*)."""
+
+    def __init__(self, device=0, stream=None, lanes=0):
+        self._lib = load()
+        h = C.c_void_p()
+        _check(self._lib.isar_batch_create(C.byref(h), device, C.c_void_p(stream) if stream else None, lanes),
+               "isar_batch_create")
+        self._h = h
+
+    @staticmethod
+    def frames(items):
+        """items: iterable of (radar, d_echo, d_velocity, flags, d_img)."""
+        items = list(items)
+        arr = (BatchFrame * len(items))()
+        for k, (rp, e, v, fl, img) in enumerate(items):
+            arr[k] = BatchFrame(rp, _dptr(e), _dptr(v), fl, _dptr(img))
+        return arr
+
+    def run(self, frames):
+        _check(self._lib.isar_batch_run(self._h, frames, len(frames)), "isar_batch_run")
+
+    def synchronize(self):
+        _check(self._lib.isar_batch_synchronize(self._h), "isar_batch_synchronize")
+
+    def autotune(self, frames):
+        ms = C.c_float()
+        _check(self._lib.isar_batch_autotune(self._h, frames, len(frames), C.byref(ms)), "isar_batch_autotune")
+        return ms.value
+
+    def lanes(self):
+        return int(self._lib.isar_batch_lanes(self._h))
+
+    def set_tuning(self, rp, t):
+        _check(self._lib.isar_batch_set_tuning(self._h, C.byref(rp), C.byref(t)), "isar_batch_set_tuning")
+
+    def tuning(self, rp):
+        t = Tuning()
+        _check(self._lib.isar_batch_get_tuning(self._h, C.byref(rp), C.byref(t)), "isar_batch_get_tuning")
+        return t
+
+    @property
+    def stream(self):
+        return self._lib.isar_batch_stream(self._h)
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self._lib.isar_batch_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()

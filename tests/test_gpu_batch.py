@@ -1,0 +1,91 @@
+"""Batched imaging (one CUDA graph over frames of uneven size) and the
+autotuner, through the C ABI: equal to single-frame imaging with the same
+launch parameters, and to the FP64 oracle."""
+import numpy as np
+import pytest
+
+import oracle
+from tests.helpers import make_frame, rel_l2
+from tests.test_gpu_parity import TOL_RA_FREE
+
+pytestmark = pytest.mark.gpu
+
+# (M, N, full, seed): uneven pulse and range-cell counts, plain and
+# five-stage frames mixed, two frames sharing each of two shapes
+FRAMES = [(128, 512, False, 41), (256, 1024, False, 42), (128, 1024, False, 43), (256, 1024, False, 44),
+          (128, 512, False, 45), (256, 2048, True, 46)]
+
+
+def _frames_on_device(torch, g):
+    out = []
+    for M, N, full, seed in FRAMES:
+        e, v = make_frame(M, N, seed=seed, full=full)
+        de = torch.from_numpy(np.ascontiguousarray(e, np.complex64).view(np.float32).copy()).cuda()
+        dv = torch.from_numpy(np.ascontiguousarray(v, np.float64).copy()).cuda()
+        img = torch.full((M, 512), np.nan, dtype=torch.float32, device="cuda")
+        flags = (g.FLAG_HPC | g.FLAG_MTRC) if full else 0
+        out.append(dict(M=M, N=N, full=full, e=e, v=v, de=de, dv=dv, img=img, flags=flags, rp=g.radar(M, N)))
+    return out
+
+
+def _batch_list(g, fr):
+    return g.Batch.frames((f["rp"], f["de"], f["dv"] if f["full"] else None, f["flags"], f["img"]) for f in fr)
+
+
+def test_batch_equals_single_frame_and_oracle(torch_cuda, gb300):
+    torch = torch_cuda
+    fr = _frames_on_device(torch, gb300)
+    with gb300.Batch(lanes=2) as b:
+        lst = _batch_list(gb300, fr)
+        b.run(lst)
+        b.synchronize()
+        got = [f["img"].cpu().numpy().copy() for f in fr]
+        # a replay of the cached graph gives the same images
+        for f in fr:
+            f["img"].fill_(np.nan)
+        b.run(lst)
+        b.synchronize()
+        for f, g0 in zip(fr, got):
+            assert np.array_equal(f["img"].cpu().numpy(), g0)
+        tunings = {(f["M"], f["N"]): b.tuning(f["rp"]) for f in fr}
+    for f, img in zip(fr, got):
+        t = tunings[(f["M"], f["N"])]
+        assert t.af_cluster > 0
+        with gb300.Context(f["rp"], stream=torch.cuda.current_stream().cuda_stream) as ctx:
+            ctx.set_tuning(**{k: getattr(t, k) for k in ("ra_pair_min", "ra_rows_per_cta", "ra_rows_final",
+                                                         "af_cluster", "af_tol", "af_iters")})
+            single = ctx.image_host(f["e"], f["v"], f["flags"])
+        assert rel_l2(img, single) <= 1e-6, (f["M"], f["N"])
+        want, _ = oracle.image(f["e"], f["v"], oracle.radar(f["M"], f["N"]), hpc=f["full"], mtrc=f["full"])
+        assert rel_l2(img, want) < TOL_RA_FREE, (f["M"], f["N"])
+
+
+def test_batch_autotune_keeps_results(torch_cuda, gb300):
+    torch = torch_cuda
+    fr = _frames_on_device(torch, gb300)[:4]
+    with gb300.Batch() as b:
+        lst = _batch_list(gb300, fr)
+        ms = b.autotune(lst)
+        assert 0.0 < ms < 1e4
+        assert b.lanes() in (1, 2, 4, 8, 16)
+        b.run(lst)
+        b.synchronize()
+        for f in fr:
+            t = b.tuning(f["rp"])
+            assert t.af_cluster in (4, 8, 16) and t.ra_pair_min >= 1
+    for f in fr:
+        want, _ = oracle.image(f["e"], f["v"], oracle.radar(f["M"], f["N"]), hpc=f["full"], mtrc=f["full"])
+        assert rel_l2(f["img"].cpu().numpy(), want) < TOL_RA_FREE
+
+
+def test_context_autotune_cooperative_or_cluster(torch_cuda, gb300):
+    torch = torch_cuda
+    M, N = 256, 1024
+    e, v = make_frame(M, N, seed=77)
+    de = torch.from_numpy(np.ascontiguousarray(e, np.complex64).view(np.float32).copy()).cuda()
+    want, _ = oracle.image(e, v, oracle.radar(M, N))
+    with gb300.Context(gb300.radar(M, N), stream=torch.cuda.current_stream().cuda_stream) as ctx:
+        t = ctx.autotune(de, None, 0, engines=3)
+        assert t.af_cluster in (0, 4, 8, 16)
+        got = ctx.image_host(e, v, 0)
+    assert rel_l2(got, want) < TOL_RA_FREE
