@@ -78,6 +78,9 @@ typedef struct {
     int af_iterations;        /* autofocus phase updates applied             */
     float af_entropy;         /* entropy of the U bins at the last evaluated
                                  phase (cluster engine; NaN otherwise)       */
+    int ws_used;              /* the learned warm start was kept             */
+    float af_entropy_start[2];/* entropy of the Doppler start and of the
+                                 learned start (NaN without a warm start)    */
 } isar_trace;
 
 /*
@@ -183,6 +186,10 @@ typedef struct {
     double snr_db;
     double rms_counts;        /* ADC scale of the signal part (int16 counts)      */
     uint64_t seed;
+    int phase_poly_order;     /* >= 2: add sum_{k=2..order} c_k u^k, u in [-1,1) */
+    double phase_poly_sigma;  /* rad: c_k ~ N(0, sigma), drawn per frame          */
+    double* h_phase_err;      /* out (host, M doubles, may be NULL): injected     */
+                              /* per-pulse phase error, rad                       */
 } isar_synth_params;
 
 /* Writes one M x N frame of int16-quantised counts as complex64 into d_out
@@ -259,6 +266,51 @@ ISAR_API int isar_batch_lanes(isar_batch* b);
 /* Tunes each shape (isar_autotune, cluster engine) and the lanes per shape
  * on this frame list; *best_ms (may be NULL) = the fastest batch time. */
 ISAR_API int isar_batch_autotune(isar_batch* b, const isar_batch_frame* frames, int n, float* best_ms);
+
+/* ---- learned autofocus warm start ----------------------------------------
+ * No counterpart in the reference.  A small network (6 x 1-D conv k=5, 64
+ * channels, then a per-pulse 64 -> 64 -> 2 head) reads per-pulse features of
+ * the cut (unit phasors and magnitudes of pulse-pair products on the 16
+ * strongest bins, the Doppler-tracking increment psi) and predicts the
+ * residual r of the Doppler-tracking phase increment.  The warm start
+ * phase[m+1] = exp(-j sum (psi - r)) competes with the Doppler start: the
+ * cluster engine keeps the one with the lower entropy of the selected bins.
+ * Dense layers are bf16 tcgen05 GEMMs with fp32 accumulation, for inference
+ * and training. */
+typedef struct isar_wsnet isar_wsnet;
+
+/* Number of fp32 parameters (canonical order: 6 conv layers W[64][320] with
+ * column k*64+c then b[64]; head W[64][64], b[64]; W[2][64], b[2]). */
+ISAR_API int isar_wsnet_param_count(void);
+/* max_rows = frames * pulses per call (multiple of 8); training != 0 keeps
+ * activations and gradient buffers.  Parameters start at zero. */
+ISAR_API int isar_wsnet_create(isar_wsnet** out, int max_rows, int training, int device, void* stream);
+ISAR_API int isar_wsnet_destroy(isar_wsnet* net);
+ISAR_API void* isar_wsnet_stream(isar_wsnet* net);
+ISAR_API int isar_wsnet_set_params(isar_wsnet* net, const float* h_params);
+ISAR_API int isar_wsnet_get_params(isar_wsnet* net, float* h_params);
+/* d_x0: bf16 [frames*M][64] features (isar_frame_features); d_out: fp32
+ * [frames*M][2] = (c, s), r = atan2(s, c); may be NULL.  Blocking. */
+ISAR_API int isar_wsnet_forward(isar_wsnet* net, const void* d_x0, int frames, int M, float* d_out);
+/* Loss 1 - |mean_m exp(j (r_hat_m - r_m))| per frame (m < M-1) of the last
+ * forward against d_target (fp32 [frames*M]); gradients into the network;
+ * *h_loss = mean over frames (may be NULL).  Blocking. */
+ISAR_API int isar_wsnet_backward(isar_wsnet* net, const float* d_target, int frames, int M, float* h_loss);
+ISAR_API int isar_wsnet_get_grads(isar_wsnet* net, float* h_grads);
+ISAR_API int isar_wsnet_adam(isar_wsnet* net, float lr);
+/* Test entry: C[M][N] = A[M][K] * B[N][K]^T, bf16 in, fp32 out, tensor cores. */
+ISAR_API int isar_nn_gemm_bf16(const void* A, int lda, const void* B, int ldb, float* C, int ldc, int M, int N, int K,
+                               int splits, void* stream);
+
+/* Attaches `net` (NULL detaches) as this context's warm start; needs the
+ * cluster autofocus engine.  The network must outlive the attachment and
+ * must not be trained while frames that use it are in flight. */
+ISAR_API int isar_set_warmstart(isar_ctx* ctx, const isar_wsnet* net);
+/* Training data: range alignment, centring, cut and the bin selection of a
+ * frame, then its features d_x0 (bf16 [M][64]) and psi (fp32 [M]).
+ * Stream-ordered on the context stream. */
+ISAR_API int isar_frame_features(isar_ctx* ctx, const float* d_echo, const double* d_velocity, int flags, void* d_x0,
+                                 float* d_psi);
 
 /* Batched unnormalised row FFTs of length n (512..8192) in place, for tests. */
 ISAR_API int isar_fft_rows(isar_ctx* ctx, float* d_x, int rows, int n, int inverse);

@@ -33,7 +33,10 @@ EXPORTS = ("isar_get_last_error", "isar_version", "isar_create", "isar_destroy",
            "isar_synchronize", "isar_set_ra_shifts", "isar_center_cut_noalloc", "isar_get_tuning",
            "isar_set_tuning", "isar_autotune", "isar_batch_create", "isar_batch_destroy", "isar_batch_stream",
            "isar_batch_run", "isar_batch_synchronize", "isar_batch_set_tuning", "isar_batch_get_tuning",
-           "isar_batch_lanes", "isar_batch_autotune")
+           "isar_batch_lanes", "isar_batch_autotune", "isar_wsnet_param_count", "isar_wsnet_create",
+           "isar_wsnet_destroy", "isar_wsnet_stream", "isar_wsnet_set_params", "isar_wsnet_get_params",
+           "isar_wsnet_forward", "isar_wsnet_backward", "isar_wsnet_get_grads", "isar_wsnet_adam",
+           "isar_nn_gemm_bf16", "isar_set_warmstart", "isar_frame_features")
 
 
 class IsarError(RuntimeError):
@@ -51,7 +54,8 @@ class SynthParams(C.Structure):
                 ("Fs", C.c_double), ("n_scat", C.c_int), ("patch_x", C.c_double), ("patch_y", C.c_double),
                 ("omega", C.c_double), ("r0_cells", C.c_double), ("drift_sigma", C.c_double),
                 ("phase_uniform", C.c_double), ("phase_quad", C.c_double), ("v0", C.c_double),
-                ("accel", C.c_double), ("snr_db", C.c_double), ("rms_counts", C.c_double), ("seed", C.c_uint64)]
+                ("accel", C.c_double), ("snr_db", C.c_double), ("rms_counts", C.c_double), ("seed", C.c_uint64),
+                ("phase_poly_order", C.c_int), ("phase_poly_sigma", C.c_double), ("h_phase_err", C.c_void_p)]
 
 
 class Trace(C.Structure):
@@ -59,7 +63,7 @@ class Trace(C.Structure):
                 ("center_shift", C.c_int), ("cut_offset", C.c_int), ("center_idx1_len", C.c_int),
                 ("center_idx2_len", C.c_int), ("center_threshold", C.c_float), ("tgt_num", C.c_int),
                 ("unit2_num", C.c_int), ("bins", C.c_int * 512), ("af_iterations", C.c_int),
-                ("af_entropy", C.c_float)]
+                ("af_entropy", C.c_float), ("ws_used", C.c_int), ("af_entropy_start", C.c_float * 2)]
 
 
 class Tuning(C.Structure):
@@ -124,6 +128,19 @@ def load(build_if_missing=True):
         "isar_batch_get_tuning": (i, [vp, C.POINTER(Radar), C.POINTER(Tuning)]),
         "isar_batch_lanes": (i, [vp]),
         "isar_batch_autotune": (i, [vp, vp, i, C.POINTER(C.c_float)]),
+        "isar_wsnet_param_count": (i, []),
+        "isar_wsnet_create": (i, [C.POINTER(vp), i, i, i, vp]),
+        "isar_wsnet_destroy": (i, [vp]),
+        "isar_wsnet_stream": (vp, [vp]),
+        "isar_wsnet_set_params": (i, [vp, vp]),
+        "isar_wsnet_get_params": (i, [vp, vp]),
+        "isar_wsnet_forward": (i, [vp, vp, i, i, vp]),
+        "isar_wsnet_backward": (i, [vp, vp, i, i, C.POINTER(C.c_float)]),
+        "isar_wsnet_get_grads": (i, [vp, vp]),
+        "isar_wsnet_adam": (i, [vp, C.c_float]),
+        "isar_nn_gemm_bf16": (i, [vp, i, vp, i, vp, i, i, i, i, i, vp]),
+        "isar_set_warmstart": (i, [vp, vp]),
+        "isar_frame_features": (i, [vp, vp, vp, i, vp, vp]),
     }
     for name, (res, args) in sig.items():
         f = getattr(lib, name)
@@ -186,13 +203,17 @@ def synth_params(M, N, seed, full=False, **kw):
     return SynthParams(M=M, N=N, seed=seed, **d)
 
 
-def synth_device(p: SynthParams, d_out, d_vel=None, stream=None):
-    """Generates one frame on the device; returns the host velocities (numpy)."""
+def synth_device(p: SynthParams, d_out, d_vel=None, stream=None, phase_err=False):
+    """Generates one frame on the device; returns the host velocities (numpy)
+    and, with phase_err=True, also the injected per-pulse phase error (rad)."""
     import numpy as np
     hv = np.zeros(p.M, np.float64)
+    pe = np.zeros(p.M, np.float64) if phase_err else None
+    p.h_phase_err = pe.ctypes.data if phase_err else None
     _check(load().isar_synth_device(C.byref(p), _dptr(d_out), _dptr(d_vel), hv.ctypes.data,
                                     C.c_void_p(stream) if stream else None), "isar_synth_device")
-    return hv
+    p.h_phase_err = None
+    return (hv, pe) if phase_err else hv
 
 
 class Context:
@@ -274,7 +295,8 @@ class Context:
                     cut_offset=t.cut_offset, center_idx1_len=t.center_idx1_len,
                     center_idx2_len=t.center_idx2_len, center_threshold=t.center_threshold,
                     tgt_num=t.tgt_num, unit2_num=U, bins=np.array(t.bins[:min(U, 512)], np.int32),
-                    af_iterations=t.af_iterations, af_entropy=t.af_entropy)
+                    af_iterations=t.af_iterations, af_entropy=t.af_entropy, ws_used=t.ws_used,
+                    af_entropy_start=(t.af_entropy_start[0], t.af_entropy_start[1]))
 
     def tuning(self):
         t = Tuning()
@@ -318,6 +340,96 @@ class Context:
         _check(self._lib.isar_autotune(self._h, _dptr(d_echo), _dptr(d_velocity), flags, engines, C.byref(t)),
                "isar_autotune")
         return t
+
+    def features(self, d_echo, d_velocity, flags, d_x0, d_psi):
+        """isar_frame_features: warm-start network inputs of one frame."""
+        _check(self._lib.isar_frame_features(self._h, _dptr(d_echo), _dptr(d_velocity), flags, _dptr(d_x0),
+                                             _dptr(d_psi)), "isar_frame_features")
+
+    def set_warmstart(self, net):
+        """Attaches a WSNet as the autofocus warm start (None detaches)."""
+        _check(self._lib.isar_set_warmstart(self._h, net._h if net is not None else None), "isar_set_warmstart")
+        self._ws = net
+
+
+class WSNet:
+    """The learned autofocus warm-start network (isar_wsnet_*)."""
+
+    def __init__(self, max_rows, training=False, device=0, stream=None):
+        self._lib = load()
+        h = C.c_void_p()
+        _check(self._lib.isar_wsnet_create(C.byref(h), int(max_rows), 1 if training else 0, device,
+                                           C.c_void_p(stream) if stream else None), "isar_wsnet_create")
+        self._h = h
+        self.n_params = int(self._lib.isar_wsnet_param_count())
+
+    @property
+    def stream(self):
+        return self._lib.isar_wsnet_stream(self._h)
+
+    def set_params(self, p):
+        import numpy as np
+        p = np.ascontiguousarray(p, np.float32)
+        assert p.size == self.n_params
+        _check(self._lib.isar_wsnet_set_params(self._h, p.ctypes.data), "isar_wsnet_set_params")
+
+    def params(self):
+        import numpy as np
+        p = np.zeros(self.n_params, np.float32)
+        _check(self._lib.isar_wsnet_get_params(self._h, p.ctypes.data), "isar_wsnet_get_params")
+        return p
+
+    def grads(self):
+        import numpy as np
+        g = np.zeros(self.n_params, np.float32)
+        _check(self._lib.isar_wsnet_get_grads(self._h, g.ctypes.data), "isar_wsnet_get_grads")
+        return g
+
+    def forward(self, d_x0, frames, M, d_out=None):
+        _check(self._lib.isar_wsnet_forward(self._h, _dptr(d_x0), frames, M, _dptr(d_out)), "isar_wsnet_forward")
+
+    def backward(self, d_target, frames, M):
+        loss = C.c_float()
+        _check(self._lib.isar_wsnet_backward(self._h, _dptr(d_target), frames, M, C.byref(loss)),
+               "isar_wsnet_backward")
+        return loss.value
+
+    def adam(self, lr):
+        _check(self._lib.isar_wsnet_adam(self._h, C.c_float(lr)), "isar_wsnet_adam")
+
+    def save(self, path):
+        import numpy as np
+        np.save(path, self.params())
+
+    def load_params(self, path):
+        import numpy as np
+        self.set_params(np.load(path))
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self._lib.isar_wsnet_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+
+def gemm_bf16(d_a, lda, d_b, ldb, d_c, ldc, M, N, K, splits=1, stream=None):
+    """Tensor-core test GEMM: C[M][N] = A[M][K] B[N][K]^T (bf16 in, fp32 out)."""
+    _check(load().isar_nn_gemm_bf16(_dptr(d_a), lda, _dptr(d_b), ldb, _dptr(d_c), ldc, M, N, K, splits,
+                                    C.c_void_p(stream) if stream else None), "isar_nn_gemm_bf16")
+
+
+WARMSTART_WEIGHTS = os.path.join(os.path.dirname(os.path.abspath(__file__)), "weights", "warmstart.npy")
 
 
 class BatchFrame(C.Structure):

@@ -7,6 +7,7 @@
 
 #include "fft.cuh"
 #include "isar_kernels.h"
+#include "nn.h"
 
 namespace isar {
 
@@ -464,7 +465,9 @@ struct AFFrame {
     const int* bins;       // [U]
     const int* fdec;       // [1] = U
     float2* phase;         // [M] in: start phase, out: final phase
-    int* stat;             // [0] iterations applied, [1] entropy bits; may be null
+    int* stat;             // [0] iterations applied, [1] entropy bits, [2] alt start used,
+                           // [3], [4] entropy bits of the two starts; may be null
+    const float2* alt;     // [M] second start phase (learned warm start) or null
 };
 
 template <int M>
@@ -511,12 +514,12 @@ k_af_cluster(AFFrame f, int iters, float tol, const float2* __restrict__ tw)
 
     const float invM = 1.0f / (float)M;
     const int rows = M / CL;
-    float e_prev = 0.0f;   // meaningful in thread 0
-    int used = iters;
-#pragma unroll 1
-    for (int it = 0; it < iters; ++it) {
-        for (int m = tid; m < M; m += A::THREADS) P[m] = make_float2(0.0f, 0.0f);
-        float s1 = 0.0f, s2 = 0.0f;
+
+    // One sweep over this CTA's bins with the phase in ph: entropy sums
+    // (s1, s2) and, when `full`, the partial row sums P of the update.
+    auto sweep = [&](bool full, float& s1, float& s2) {
+        if (full)
+            for (int m = tid; m < M; m += A::THREADS) P[m] = make_float2(0.0f, 0.0f);
 #pragma unroll 1
         for (int j = 0; j < nch; ++j) {
             const int slot = j < A::NSLOT ? j : A::NSLOT - 1;
@@ -535,6 +538,7 @@ k_af_cluster(AFFrame f, int iters, float tol, const float2* __restrict__ tw)
                                    sm[fpad(i)] = cscale(v, sqrtf(p));
                                },
                                sm, lt, tws, valid);
+            if (!full) continue;
             team_fft<M, true>([&](int i) { return sm[fpad(i)]; },
                               [&](int i, float2 v, int) { sm[fpad(i)] = cmulc(g[i], cscale(v, invM)); }, sm, lt,
                               tws, valid);
@@ -549,6 +553,71 @@ k_af_cluster(AFFrame f, int iters, float tol, const float2* __restrict__ tw)
                 P[m] = s;
             }
         }
+    };
+
+    // Optional second start (learned warm start): keep whichever of the two
+    // starting phases has the lower entropy of the selected bins.
+    if (f.alt) {
+        float e_start[2];
+#pragma unroll 1
+        for (int k = 0; k < 2; ++k) {
+            if (k == 1) {
+                __syncthreads();
+                for (int m = tid; m < M; m += A::THREADS) ph[m] = f.alt[m];
+            }
+            float s1 = 0.0f, s2 = 0.0f;
+            sweep(false, s1, s2);
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) {
+                s1 += __shfl_xor_sync(0xffffffffu, s1, o);
+                s2 += __shfl_xor_sync(0xffffffffu, s2, o);
+            }
+            if (lane == 0) {
+                red[warp] = s1;
+                red[16 + warp] = s2;
+            }
+            __syncthreads();
+            if (tid == 0) {
+                double a1 = 0.0, a2 = 0.0;
+                for (int w = 0; w < A::THREADS / 32; ++w) {
+                    a1 += red[w];
+                    a2 += red[16 + w];
+                }
+                red[32] = a1;
+                red[33] = a2;
+            }
+            cl.sync();
+            if (tid == 0) {
+                double S1 = 0.0, S2 = 0.0;
+                for (int q = 0; q < CL; ++q) {
+                    const double* rr = cl.map_shared_rank(red, q);
+                    S1 += rr[32];
+                    S2 += rr[33];
+                }
+                red[41 + k] = logf((float)S1) - (float)S2 / (float)S1;
+            }
+            cl.sync();
+            e_start[k] = (float)red[41 + k];
+        }
+        const bool use_alt = e_start[1] < e_start[0];
+        if (!use_alt) {
+            __syncthreads();
+            for (int m = tid; m < M; m += A::THREADS) ph[m] = f.phase[m];
+        }
+        if (r == 0 && tid == 0 && f.stat) {
+            f.stat[2] = use_alt ? 1 : 0;
+            f.stat[3] = __float_as_int(e_start[0]);
+            f.stat[4] = __float_as_int(e_start[1]);
+        }
+        __syncthreads();
+    }
+
+    float e_prev = 0.0f;   // meaningful in thread 0
+    int used = iters;
+#pragma unroll 1
+    for (int it = 0; it < iters; ++it) {
+        float s1 = 0.0f, s2 = 0.0f;
+        sweep(true, s1, s2);
         // Entropy sums: float per warp, double per CTA (red[32..33]) and per
         // cluster, all by one thread (FP64 is slow on this part).
 #pragma unroll
@@ -693,7 +762,7 @@ static cudaError_t af_cluster_launch(const FEArgs& a, cudaStream_t st)
     cfg.stream = st;
     cfg.attrs = at;
     cfg.numAttrs = 1;
-    AFFrame fr{a.cut, a.bins, a.fdec, a.phase, a.af_stat};
+    AFFrame fr{a.cut, a.bins, a.fdec, a.phase, a.af_stat, a.ws_w ? a.ws_phase : nullptr};
     cudaError_t e = cudaLaunchKernelEx(&cfg, k_af_cluster<M>, fr, a.iters, a.tol, a.tw);
     if (e == cudaSuccess) ISAR_COUNT(1);
     return e;
@@ -751,6 +820,15 @@ static cudaError_t fe_run_m(const FEArgs& a, cudaStream_t st)
     ISAR_COUNT(1);
     k_fe_phase<<<1, 1024, 0, st>>>(nullptr, 0, a.dsum, M, a.phase, a.fdec);
     ISAR_COUNT(1);
+    if (a.pre_only) return cudaGetLastError();
+    if (a.ws_w && (a.af_cluster == 0 || a.iters == 0)) return cudaErrorInvalidValue;
+    if (a.ws_w) {
+        // learned warm start: features -> network -> second start phase
+        cudaError_t e;
+        if ((e = nn::features(a.cut, a.E, a.dsum, M, a.ws_a->act[0], a.ws_psi, st))) return e;
+        if ((e = nn::forward(*a.ws_w, *a.ws_a, 1, M, a.ws_err, st))) return e;
+        if ((e = nn::ws_phase(a.ws_psi, a.ws_a->out, M, a.ws_phase, st))) return e;
+    }
     if (a.iters > 0 && a.af_cluster > 0) {
         cudaError_t e = af_cluster_launch<M>(a, st);
         if (e) return e;

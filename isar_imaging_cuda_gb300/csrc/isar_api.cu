@@ -21,8 +21,12 @@
 #include "isar_common.cuh"
 #include "isar_kernels.h"
 #include "isar_synth.h"
+#include "nn.h"
 
 using isar::kRangeCut;
+
+// defined with the network's C ABI (nn_api.cu)
+const isar::nn::Weights* isar_wsnet_weights(const isar_wsnet* n);
 
 namespace {
 
@@ -183,6 +187,14 @@ struct isar_ctx {
     bool use_graphs = true;
     std::vector<CachedGraph> graphs;
     unsigned long long graph_tick = 0;
+    // learned warm start: the attached network and this context's
+    // inference buffers (M rows)
+    const isar::nn::Weights* ws_w = nullptr;
+    isar::nn::Acts ws_a;
+    float* d_ws_psi = nullptr;
+    float2* d_ws_phase = nullptr;
+    int* d_ws_err = nullptr;
+    bool ws_alloc = false;
 };
 
 namespace {
@@ -361,6 +373,13 @@ isar::FEArgs fe_args(isar_ctx* c, float2* cut, int iters)
     a.af_cluster = c->af_cluster;
     a.tol = c->af_tol;
     a.af_stat = c->d_fdec + 4;
+    if (c->ws_w) {
+        a.ws_w = c->ws_w;
+        a.ws_a = &c->ws_a;
+        a.ws_psi = c->d_ws_psi;
+        a.ws_phase = c->d_ws_phase;
+        a.ws_err = c->d_ws_err;
+    }
     return a;
 }
 
@@ -633,6 +652,9 @@ ISAR_API int isar_synth_device(const isar_synth_params* p, float* d_out, double*
     q.snr_db = p->snr_db;
     q.rms_counts = p->rms_counts;
     q.seed = p->seed;
+    q.phase_poly_order = p->phase_poly_order;
+    q.phase_poly_sigma = p->phase_poly_sigma;
+    q.h_phase_err = p->h_phase_err;
     int64_t* scratch = nullptr;
     CU(cudaMalloc(&scratch, (size_t)p->M * (p->n_scat > 0 ? p->n_scat : 1) * 4 * sizeof(int64_t)));
     cudaError_t e = isar::synth_frame(q, reinterpret_cast<float2*>(d_out), d_velocity, h_velocity, scratch,
@@ -671,6 +693,59 @@ ISAR_API int isar_get_trace(isar_ctx* c, isar_trace* t)
         t->af_iterations = c->af_iters;
         t->af_entropy = NAN;
     }
+    t->ws_used = c->ws_w ? fdec[6] : 0;
+    if (c->ws_w) {
+        std::memcpy(&t->af_entropy_start[0], &fdec[7], sizeof(float));
+        std::memcpy(&t->af_entropy_start[1], &fdec[8], sizeof(float));
+    } else {
+        t->af_entropy_start[0] = t->af_entropy_start[1] = NAN;
+    }
+    return ISAR_OK;
+}
+
+ISAR_API int isar_set_warmstart(isar_ctx* c, const isar_wsnet* net)
+{
+    TRY(check_ctx(c));
+    if (net && c->af_cluster == 0)
+        return fail(ISAR_EINVAL, "the learned warm start needs the cluster autofocus engine (isar_set_tuning)");
+    CU(cudaStreamSynchronize(c->st));
+    if (net && !c->ws_alloc) {
+        const size_t M = c->M;
+        c->ws_a.rows = c->M;
+        for (int l = 0; l < isar::nn::kConv + 2; ++l) TRY(dalloc(c, &c->ws_a.act[l], M * isar::nn::kCh));
+        TRY(dalloc(c, &c->ws_a.col, M * isar::nn::kColK));
+        TRY(dalloc(c, &c->ws_a.z, M * isar::nn::kCh));
+        TRY(dalloc(c, &c->ws_a.out, M * isar::nn::kOutPad));
+        TRY(dalloc(c, &c->d_ws_psi, M));
+        TRY(dalloc(c, &c->d_ws_phase, M));
+        TRY(dalloc(c, &c->d_ws_err, 1));
+        CU(cudaMemsetAsync(c->d_ws_err, 0, sizeof(int), c->st));
+        c->ws_alloc = true;
+    }
+    c->ws_w = net ? isar_wsnet_weights(net) : nullptr;
+    for (auto& g : c->graphs) cudaGraphExecDestroy(g.exec);
+    c->graphs.clear();
+    return ISAR_OK;
+}
+
+ISAR_API int isar_frame_features(isar_ctx* c, const float* d_echo, const double* d_velocity, int flags, void* d_x0,
+                                 float* d_psi)
+{
+    TRY(check_ctx(c));
+    if (!d_echo || !d_x0 || !d_psi) return fail(ISAR_EINVAL, "null argument");
+    const float2* x = reinterpret_cast<const float2*>(d_echo);
+    if (c->r.data_type == ISAR_DATA_IFDS) {
+        CU(cudaMemcpyAsync(c->d_in, x, (size_t)c->M * c->N * sizeof(float2), cudaMemcpyDeviceToDevice, c->st));
+        CU(isar::ifds_pre(c->d_in, c->M, c->N, c->d_tw, c->st));
+        x = c->d_in;
+    }
+    TRY(run_range_align(c, x, c->d_x, d_velocity, flags));
+    CU(isar::center_cut(c->d_arp, c->d_x, c->M, c->N, c->d_dec, c->d_cut, c->st));
+    isar::FEArgs a = fe_args(c, c->d_cut, 0);
+    a.ws_w = nullptr;
+    a.pre_only = 1;
+    CU(isar::fe_run(a, c->st));
+    CU(isar::nn::features(c->d_cut, c->d_E, c->d_dsum, c->M, static_cast<__nv_bfloat16*>(d_x0), d_psi, c->st));
     return ISAR_OK;
 }
 
@@ -702,6 +777,7 @@ ISAR_API int isar_set_tuning(isar_ctx* c, const isar_tuning* t)
                     isar::af_cluster_max(c->M));
     if (t->af_tol < 0.0f || !(t->af_tol < 1.0f)) return fail(ISAR_EINVAL, "af_tol must be in [0, 1)");
     if (t->af_tol > 0.0f && t->af_cluster == 0) return fail(ISAR_EINVAL, "af_tol needs the cluster engine");
+    if (c->ws_w && t->af_cluster == 0) return fail(ISAR_EINVAL, "the attached warm start needs the cluster engine");
     if (t->af_iters < 0 || t->af_iters > 100000) return fail(ISAR_EINVAL, "af_iters out of range");
     CU(cudaStreamSynchronize(c->st));
     c->ra_pair_min = t->ra_pair_min;

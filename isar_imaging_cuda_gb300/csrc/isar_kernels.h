@@ -8,6 +8,11 @@
 
 namespace isar {
 
+namespace nn {
+struct Weights;
+struct Acts;
+}  // namespace nn
+
 // Number of kernels this library has launched (all contexts).
 inline std::atomic<long long>& launch_counter()
 {
@@ -59,7 +64,15 @@ struct FEArgs {
     // selected bins changes by <= tol * |entropy| between two iterations;
     // 0 runs all `iters` (the reference's fixed count).
     float tol;
-    int* af_stat;            // [0] iterations applied, [1] entropy (float bits); may be null
+    int* af_stat;            // [0] iterations applied, [1] entropy (float bits), [2] warm start used,
+                             // [3], [4] start entropies (float bits); may be null
+    // Learned warm start (cluster engine only), or ws_w == nullptr.
+    const nn::Weights* ws_w;
+    nn::Acts* ws_a;          // inference activations for M rows; act[0] receives the features
+    float* ws_psi;           // [M]
+    float2* ws_phase;        // [M] warm-start phase
+    int* ws_err;             // GEMM wait-timeout flag
+    int pre_only;            // stop after the bin selection and the Doppler start phase
 };
 
 // Largest cluster the device accepts for the autofocus engine with M pulses

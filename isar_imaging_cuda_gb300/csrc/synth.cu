@@ -107,12 +107,25 @@ cudaError_t synth_frame(const SynthParams& p, float2* d_out, double* d_vel, doub
     }
     std::vector<int64_t> coef((size_t)M * K * 4);
     std::vector<double> vel(M);
+    // polynomial phase-error coefficients from their own stream, so that
+    // frames without them are unchanged
+    double poly[8] = {0.0};
+    if (p.phase_poly_order >= 2) {
+        Rng prng{p.seed ^ 0x5DEECE66Dull};
+        for (int k = 2; k <= p.phase_poly_order && k < 8; ++k) poly[k] = p.phase_poly_sigma * prng.gauss();
+    }
     double d = 0.0;
     for (int m = 0; m < M; ++m) {
         const double drift = d * cell;
         d += p.drift_sigma * rng.gauss();
         const double u = (double)(m - M / 2) / (double)(M / 2);
-        const double perr = p.phase_quad * u * u + p.phase_uniform * (2.0 * rng.uniform() - 1.0);
+        double perr = p.phase_quad * u * u + p.phase_uniform * (2.0 * rng.uniform() - 1.0);
+        double uk = u;
+        for (int k = 2; k < 8; ++k) {
+            uk *= u;
+            perr += poly[k] * uk;
+        }
+        if (p.h_phase_err) p.h_phase_err[m] = perr;
         const double v = p.v0 + p.accel * (double)m / p.prf;
         vel[m] = (double)std::llround(v * 10.0) * 0.1;   // navigation header, 0.1 m/s
         const double th = p.omega * (double)(m - M / 2) / p.prf;

@@ -1,0 +1,77 @@
+"""The warm-start network's CUDA kernels through the C ABI: the tcgen05 bf16
+GEMM against an FP64 matmul, and forward / loss / gradients against the
+CPU restatement (oracle/wsnet.py, same bf16 rounding points)."""
+import numpy as np
+import pytest
+
+from oracle import wsnet
+
+pytestmark = pytest.mark.gpu
+
+
+def _bf16_tensor(torch, x):
+    return torch.from_numpy(wsnet.bf16(np.asarray(x, np.float32))).cuda().to(torch.bfloat16)
+
+
+@pytest.mark.parametrize("M,N,K,splits", [(256, 64, 320, 1), (300, 16, 64, 1), (320, 64, 4096, 8),
+                                          (128, 320, 64, 1), (200, 16, 1024, 3)])
+def test_gemm_bf16_matches_fp64(torch_cuda, gb300, M, N, K, splits):
+    torch = torch_cuda
+    rng = np.random.default_rng(M + N + K)
+    a = _bf16_tensor(torch, rng.standard_normal((M, K)))
+    b = _bf16_tensor(torch, rng.standard_normal((N, K)))
+    c = torch.full((M, N), np.nan, dtype=torch.float32, device="cuda")
+    gb300.gemm_bf16(a, K, b, K, c, N, M, N, K, splits)
+    torch.cuda.synchronize()
+    want = a.double() @ b.double().T
+    err = float((c.double() - want).norm() / want.norm())
+    assert err < 1e-5, err
+
+
+def _setup(torch, F, M, seed):
+    rng = np.random.default_rng(seed)
+    p = wsnet.init_params(seed, out_scale=0.3)
+    x0 = wsnet.bf16(rng.standard_normal((F, M, wsnet.CH)).astype(np.float32) * 0.7)
+    target = rng.uniform(-1.5, 1.5, (F, M)).astype(np.float32)
+    dx = torch.from_numpy(x0).cuda().to(torch.bfloat16).contiguous()
+    dt = torch.from_numpy(target).cuda()
+    return p, x0, target, dx, dt
+
+
+def test_forward_loss_and_grads_match_oracle(torch_cuda, gb300):
+    torch = torch_cuda
+    F, M = 4, 64
+    p, x0, target, dx, dt = _setup(torch, F, M, 3)
+    with gb300.WSNet(F * M, training=True) as net:
+        net.set_params(p)
+        out = torch.empty((F * M, 2), dtype=torch.float32, device="cuda")
+        net.forward(dx, F, M, out)
+        loss = net.backward(dt, F, M)
+        g = net.grads()
+    want_out, _ = wsnet.forward(p, x0, emulate=True)
+    got = out.cpu().numpy().reshape(F, M, 2)
+    assert np.linalg.norm(got - want_out) / np.linalg.norm(want_out) < 2e-3
+    want_loss, want_g = wsnet.loss_grad(p, x0, target, emulate=True)
+    assert abs(loss - want_loss) < 1e-4
+    o = 0
+    for li, (r, c) in enumerate(wsnet.layer_shapes()):
+        for name, n in (("W", r * c), ("b", r)):
+            a, w = g[o:o + n].astype(np.float64), want_g[o:o + n]
+            o += n
+            rel = np.linalg.norm(a - w) / max(np.linalg.norm(w), 1e-30)
+            cos = float(a @ w / max(np.linalg.norm(a) * np.linalg.norm(w), 1e-30))
+            assert rel < 3e-2 and cos > 0.999, (li, name, rel, cos)
+
+
+def test_adam_steps_reduce_loss(torch_cuda, gb300):
+    torch = torch_cuda
+    F, M = 8, 64
+    p, x0, target, dx, dt = _setup(torch, F, M, 5)
+    with gb300.WSNet(F * M, training=True) as net:
+        net.set_params(p)
+        losses = []
+        for _ in range(30):
+            net.forward(dx, F, M)
+            losses.append(net.backward(dt, F, M))
+            net.adam(3e-3)
+    assert losses[-1] < 0.5 * losses[0], losses
