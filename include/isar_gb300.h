@@ -188,8 +188,9 @@ typedef struct {
     uint64_t seed;
     int phase_poly_order;     /* >= 2: add sum_{k=2..order} c_k u^k, u in [-1,1) */
     double phase_poly_sigma;  /* rad: c_k ~ N(0, sigma), drawn per frame          */
-    double* h_phase_err;      /* out (host, M doubles, may be NULL): injected     */
-                              /* per-pulse phase error, rad                       */
+    double* h_phase_err;      /* out (host, M doubles, may be NULL): per-pulse    */
+                              /* phase to remove, rad: the injected error plus    */
+                              /* the carrier phase of the range drift             */
 } isar_synth_params;
 
 /* Writes one M x N frame of int16-quantised counts as complex64 into d_out

@@ -125,7 +125,9 @@ cudaError_t synth_frame(const SynthParams& p, float2* d_out, double* d_vel, doub
             uk *= u;
             perr += poly[k] * uk;
         }
-        if (p.h_phase_err) p.h_phase_err[m] = perr;
+        // the phase the autofocus has to remove: the injected error plus the
+        // carrier phase of the translational range drift, -4 pi fc drift / c
+        if (p.h_phase_err) p.h_phase_err[m] = perr - 4.0 * M_PI * p.fc * drift / c;
         const double v = p.v0 + p.accel * (double)m / p.prf;
         vel[m] = (double)std::llround(v * 10.0) * 0.1;   // navigation header, 0.1 m/s
         const double th = p.omega * (double)(m - M / 2) / p.prf;
