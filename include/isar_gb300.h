@@ -101,6 +101,7 @@ typedef struct {
 } isar_tuning;
 
 typedef struct isar_ctx isar_ctx;
+typedef struct isar_wsnet isar_wsnet;   /* learned warm-start network, see below */
 
 /* Copies the calling thread's last error message; returns its length. */
 ISAR_API int isar_get_last_error(char* buf, size_t len);
@@ -264,6 +265,9 @@ ISAR_API int isar_batch_synchronize(isar_batch* b);
 ISAR_API int isar_batch_set_tuning(isar_batch* b, const isar_radar* shape, const isar_tuning* t);
 ISAR_API int isar_batch_get_tuning(isar_batch* b, const isar_radar* shape, isar_tuning* out);
 ISAR_API int isar_batch_lanes(isar_batch* b);
+/* Attaches `net` (NULL detaches) as the warm start of every lane, present
+ * and future (isar_set_warmstart); drops cached graphs. */
+ISAR_API int isar_batch_set_warmstart(isar_batch* b, const isar_wsnet* net);
 /* Tunes each shape (isar_autotune, cluster engine) and the lanes per shape
  * on this frame list; *best_ms (may be NULL) = the fastest batch time. */
 ISAR_API int isar_batch_autotune(isar_batch* b, const isar_batch_frame* frames, int n, float* best_ms);
@@ -278,7 +282,6 @@ ISAR_API int isar_batch_autotune(isar_batch* b, const isar_batch_frame* frames, 
  * cluster engine keeps the one with the lower entropy of the selected bins.
  * Dense layers are bf16 tcgen05 GEMMs with fp32 accumulation, for inference
  * and training. */
-typedef struct isar_wsnet isar_wsnet;
 
 /* Number of fp32 parameters (canonical order: 6 conv layers W[64][320] with
  * column k*64+c then b[64]; head W[64][64], b[64]; W[2][64], b[2]). */

@@ -36,7 +36,7 @@ EXPORTS = ("isar_get_last_error", "isar_version", "isar_create", "isar_destroy",
            "isar_batch_lanes", "isar_batch_autotune", "isar_wsnet_param_count", "isar_wsnet_create",
            "isar_wsnet_destroy", "isar_wsnet_stream", "isar_wsnet_set_params", "isar_wsnet_get_params",
            "isar_wsnet_forward", "isar_wsnet_backward", "isar_wsnet_get_grads", "isar_wsnet_adam",
-           "isar_nn_gemm_bf16", "isar_set_warmstart", "isar_frame_features")
+           "isar_nn_gemm_bf16", "isar_set_warmstart", "isar_frame_features", "isar_batch_set_warmstart")
 
 
 class IsarError(RuntimeError):
@@ -141,6 +141,7 @@ def load(build_if_missing=True):
         "isar_nn_gemm_bf16": (i, [vp, i, vp, i, vp, i, i, i, i, i, vp]),
         "isar_set_warmstart": (i, [vp, vp]),
         "isar_frame_features": (i, [vp, vp, vp, i, vp, vp]),
+        "isar_batch_set_warmstart": (i, [vp, vp]),
     }
     for name, (res, args) in sig.items():
         f = getattr(lib, name)
@@ -470,6 +471,12 @@ class Batch:
 
     def lanes(self):
         return int(self._lib.isar_batch_lanes(self._h))
+
+    def set_warmstart(self, net):
+        """Attaches a WSNet as the warm start of every lane (None detaches)."""
+        _check(self._lib.isar_batch_set_warmstart(self._h, net._h if net is not None else None),
+               "isar_batch_set_warmstart")
+        self._ws = net
 
     def set_tuning(self, rp, t):
         _check(self._lib.isar_batch_set_tuning(self._h, C.byref(rp), C.byref(t)), "isar_batch_set_tuning")

@@ -94,6 +94,7 @@ struct isar_batch {
     bool own_stream = false;
     cudaEvent_t fork = nullptr;
     int lanes = 4;                 // lanes per shape (isar_batch_autotune picks it)
+    const isar_wsnet* ws = nullptr;   // learned warm start of every lane, or null
     std::vector<std::unique_ptr<Shape>> shapes;
     std::vector<BatchGraph> graphs;
     unsigned long long tick = 0;
@@ -151,6 +152,7 @@ int ensure_lanes(isar_batch* b, Shape* s, int n)
             s->tuned = true;
         }
         rc = isar_set_tuning(l.ctx, &s->tuning);
+        if (rc == ISAR_OK && b->ws) rc = isar_set_warmstart(l.ctx, b->ws);
         if (rc != ISAR_OK) {
             destroy_lane(l);
             return rc;
@@ -444,6 +446,17 @@ ISAR_API int isar_batch_get_tuning(isar_batch* b, const isar_radar* shape, isar_
 }
 
 ISAR_API int isar_batch_lanes(isar_batch* b) { return b ? b->lanes : 0; }
+
+ISAR_API int isar_batch_set_warmstart(isar_batch* b, const isar_wsnet* net)
+{
+    if (!b) return fail(ISAR_EINVAL, "null batch");
+    CU(cudaStreamSynchronize(b->st));
+    for (auto& s : b->shapes)
+        for (auto& l : s->lanes) TRY(isar_set_warmstart(l.ctx, net));
+    b->ws = net;
+    drop_graphs(b);
+    return ISAR_OK;
+}
 
 /*
  * Autotunes `f`: per shape, the launch parameters on the first frame of that
