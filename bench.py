@@ -411,6 +411,44 @@ def run_reference(args):
     print(json.dumps(out))
 
 
+def run_profile(args):
+    """Profiling workloads (no timing, no JSON): `plain` images one
+    1024 x 8192 frame warmup + steps times; `batch` runs a batch of 8
+    frames through isar_batch_run (cluster autofocus, learned warm start)."""
+    import torch
+
+    import isar_imaging_cuda_gb300 as g
+    s = torch.cuda.Stream()
+    torch.cuda.set_stream(s)
+    rp = g.radar(M, N)
+    flags = g.FLAG_HPC | g.FLAG_MTRC
+    nb = 1 if args.profile == "plain" else 8
+    X = torch.empty((nb, M, 2 * N), dtype=torch.float32, device="cuda")
+    V = torch.empty((nb, M), dtype=torch.float64, device="cuda")
+    imgs = torch.empty((nb, M, C), dtype=torch.float32, device="cuda")
+    for i in range(nb):
+        g.synth_device(g.synth_params(M, N, seed=i, full=True), X[i], V[i], s.cuda_stream)
+    if args.profile == "plain":
+        with g.Context(rp, stream=s.cuda_stream) as ctx:
+            for _ in range(args.warmup + args.steps):
+                ctx.image_device(X[0], V[0], imgs[0], flags)
+            ctx.synchronize()
+    else:
+        net = g.WSNet(M, stream=s.cuda_stream)
+        net.load_params(g.WARMSTART_WEIGHTS)
+        with g.Batch(stream=s.cuda_stream, lanes=8) as b:
+            b.set_warmstart(net)
+            b.set_tuning(rp, g.Tuning(ra_pair_min=128, ra_rows_per_cta=4, ra_rows_final=4, af_cluster=16,
+                                      af_tol=TOL, af_iters=120, af_cluster_max=0))
+            lst = g.Batch.frames((rp, X[i], V[i], flags, imgs[i]) for i in range(nb))
+            for _ in range(args.warmup + args.steps):
+                b.run(lst)
+            b.synchronize()
+        net.close()
+    torch.cuda.synchronize()
+    print("profile workload %s done" % args.profile)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -418,7 +456,12 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--profile", choices=["plain", "batch"], default=None,
+                    help="run a profiling workload only (for ncu), no measurement")
     args = ap.parse_args()
+    if args.profile:
+        run_profile(args)
+        return
     if args.warmup < 3:
         args.warmup = 3
     if args.impl == "reference":
