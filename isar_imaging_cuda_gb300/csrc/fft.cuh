@@ -96,12 +96,12 @@ struct TwGlobal {
     __device__ __forceinline__ float2 operator()(int e, int n) const { return __ldg(&p[e * (kTwN / n)]); }
 };
 
-// TwShared<N>: a per-CTA shared-memory table.  For N <= 2048 it holds all N
-// twiddles; above that a two-level table hi[e >> 6] * lo[e & 63]
+// TwShared<N>: a per-CTA shared-memory table.  For N <= 2048 (or FULL) it
+// holds all N twiddles; above that a two-level table hi[e >> 6] * lo[e & 63]
 // (N/64 + 64 entries, one extra complex multiply, ~1 ulp more rounding).
-template <int N>
+template <int N, bool FULL = false>
 struct TwShared {
-    static constexpr bool kTwoLevel = N > 2048;
+    static constexpr bool kTwoLevel = !FULL && N > 2048;
     static constexpr int kEntries = kTwoLevel ? N / 64 + 64 : N;
     const float2* p;
     __device__ __forceinline__ float2 operator()(int e, int) const
@@ -136,10 +136,13 @@ __device__ __forceinline__ void fft_pass(Src& src, Dst& dst, float2* sm, int lt,
 #pragma unroll
         for (int b = 0; b < B; ++b) {
             const int j = lt + b * T;
+            // fpad(j + r*K) = fpad(j) + r*K*17/16 when K is a multiple of 16
+            const int pj = fpad(j);
 #pragma unroll
             for (int r = 0; r < R; ++r) {
                 const int idx = j + r * (N / R);
                 if constexpr (FIRST) v[b * R + r] = src(idx);
+                else if constexpr ((N / R) % 16 == 0) v[b * R + r] = sm[pj + r * ((N / R) + (N / R) / 16)];
                 else v[b * R + r] = sm[fpad(idx)];
             }
         }
@@ -162,10 +165,13 @@ __device__ __forceinline__ void fft_pass(Src& src, Dst& dst, float2* sm, int lt,
             }
             dft_reg<R, INV>(&v[b * R]);
             const int base = (j / NS) * NS * R + k;
+            const int pb = fpad(base);
 #pragma unroll
             for (int r = 0; r < R; ++r) {
                 const int idx = base + r * NS;
                 if constexpr (LAST) dst(idx, v[b * R + r], b * R + r);
+                else if constexpr (NS % 16 == 0) sm[pb + r * (NS + NS / 16)] = v[b * R + r];
+                else if constexpr (NS == 1 && R == 16) sm[pb + r] = v[b * R + r];   // base = 16 j
                 else sm[fpad(idx)] = v[b * R + r];
             }
         }

@@ -34,6 +34,13 @@ __device__ __forceinline__ float2 row_phase(int64_t hq, int64_t sq, int n)
     return cis_frac64(ph);
 }
 
+// Twiddle table of the range-alignment kernels: the two-level shared table
+// above 2048 points.  (A full N-entry table is read with strides of 32 words
+// by the radix-16 passes, i.e. with many-way bank conflicts; the two-level
+// table's hi/lo lookups spread or broadcast across a warp.)
+template <int N>
+using RaTw = TwShared<N>;
+
 // HPC coefficient per pulse: alpha_m = coef * v_m / Fs^2 in cycles per n^2,
 // coef = -4*pi*(B/Tp)/c (high_speed_compensation.cu:17-18).
 __global__ void k_hpc_coef(const double* __restrict__ vel, int M, double coef_over_fs2, int64_t* __restrict__ hq)
@@ -292,9 +299,9 @@ k_ra_pair(const float2* __restrict__ x, const float* __restrict__ win, const int
     const int j = blockIdx.x;
     float2* sm = reinterpret_cast<float2*>(sm_f);
     float2* twt = reinterpret_cast<float2*>(eb + N);
-    TwShared<N>::fill(twt, tw, lt, F::T);
+    RaTw<N>::fill(twt, tw, lt, F::T);
     __syncthreads();
-    const TwShared<N> tws{twt};
+    const RaTw<N> tws{twt};
 #pragma unroll 1
     for (int g = 0; g < 2; ++g) {
         const int k = 2 * j + g;
@@ -344,9 +351,9 @@ k_ra_accum(const float2* __restrict__ x, const float* __restrict__ win, const in
     const int k = blockIdx.x / nch, q = blockIdx.x % nch;
     const int r0 = k * s + s / 2 + q * rpc;
     float2* twt = sm + F::SMEM;
-    TwShared<N>::fill(twt, tw, lt, F::T);
+    RaTw<N>::fill(twt, tw, lt, F::T);
     __syncthreads();
-    const TwShared<N> tws{twt};
+    const RaTw<N> tws{twt};
     float acc[16], accl[16];
 #pragma unroll
     for (int t = 0; t < 16; ++t) acc[t] = accl[t] = 0.0f;
@@ -387,10 +394,10 @@ k_ra_corr(const float* __restrict__ E, double* __restrict__ S, int64_t* __restri
     const int j = blockIdx.x;
     const int s = 1 << level;
     float2* twt = reinterpret_cast<float2*>(ea + 2 * N);
-    TwShared<N>::fill(twt, tw, lt, F::T);
+    RaTw<N>::fill(twt, tw, lt, F::T);
     for (int i = lt; i < 2 * N; i += F::T) ea[i] = E[(size_t)2 * j * N + i];
     __syncthreads();
-    const float shc = ra_correlate<N>(ea, sm_f, lt, TwShared<N>{twt});
+    const float shc = ra_correlate<N>(ea, sm_f, lt, RaTw<N>{twt});
     const float sh = given ? shift_out[j] : shc;
     if (lt == 0 && !given) shift_out[j] = sh;
     for (int m = lt; m < s; m += F::T) add_shift(S, SQ, (size_t)(2 * j + 1) * s + m, sh, N);
@@ -413,9 +420,9 @@ k_ra_final(const float2* x, float2* yout, const float* __restrict__ win, const i
     const int r0 = blockIdx.x * rpc;
     const float invN = 1.0f / (float)N;
     float2* twt = sm + F::SMEM;
-    TwShared<N>::fill(twt, tw, lt, F::T);
+    RaTw<N>::fill(twt, tw, lt, F::T);
     __syncthreads();
-    const TwShared<N> tws{twt};
+    const RaTw<N> tws{twt};
     float acc[16];
 #pragma unroll
     for (int t = 0; t < 16; ++t) acc[t] = 0.0f;
@@ -712,10 +719,10 @@ __global__ void __launch_bounds__(N / 16) k_fft_rows(float2* x, const float2* __
 template <int N>
 static size_t pair_smem()
 {
-    return ((size_t)FFTShape<N>::SMEM + TwShared<N>::kEntries) * sizeof(float2) + 2 * N * sizeof(float);
+    return ((size_t)FFTShape<N>::SMEM + RaTw<N>::kEntries) * sizeof(float2) + 2 * N * sizeof(float);
 }
 template <int N>
-static size_t fft_smem() { return ((size_t)FFTShape<N>::SMEM + TwShared<N>::kEntries) * sizeof(float2); }
+static size_t fft_smem() { return ((size_t)FFTShape<N>::SMEM + RaTw<N>::kEntries) * sizeof(float2); }
 
 template <int N>
 static cudaError_t set_attrs()
