@@ -461,8 +461,9 @@ ISAR_API int isar_batch_set_warmstart(isar_batch* b, const isar_wsnet* net)
 /*
  * Autotunes `f`: per shape, the launch parameters on the first frame of that
  * shape (isar_autotune with the cluster engine only), then the lanes per
- * shape from {1, 2, 4, 8, 16} (up to the largest frame count of a shape) by
- * timing whole-batch graph replays.  Leaves the fastest graph cached.
+ * shape from {1, 2, 4, 8, 16, 32} (up to the largest frame count of a shape)
+ * jointly with the cluster size (16 or 8 CTAs) by timing whole-batch graph
+ * replays.  The next isar_batch_run captures the chosen configuration.
  */
 ISAR_API int isar_batch_autotune(isar_batch* b, const isar_batch_frame* f, int n, float* best_ms)
 {
@@ -495,21 +496,37 @@ ISAR_API int isar_batch_autotune(isar_batch* b, const isar_batch_frame* f, int n
         s->tuning = t;
         for (auto& l : s->lanes) TRY(isar_set_tuning(l.ctx, &t));
     }
+    // lanes x cluster size on the whole batch: single-frame latency favours
+    // large clusters, concurrent lanes can favour smaller ones
+    auto apply_cluster = [&](int cl) -> int {
+        for (auto& sp : b->shapes) {
+            Shape* s = sp.get();
+            if (cl > s->tuning.af_cluster_max) continue;
+            s->tuning.af_cluster = cl;
+            for (auto& l : s->lanes) TRY(isar_set_tuning(l.ctx, &s->tuning));
+        }
+        return ISAR_OK;
+    };
     float best = 1e30f;
-    int best_l = b->lanes;
-    for (int L : {1, 2, 4, 8, 16}) {
-        if (L > 1 && L / 2 >= most) break;
-        BatchGraph g;
-        TRY(capture_batch(b, f, n, L, &g));
-        float ms = 0.0f;
-        const int rc = time_graph(b, g.exec, 3, &ms);
-        cudaGraphExecDestroy(g.exec);
-        TRY(rc);
-        if (ms < best) {
-            best = ms;
-            best_l = L;
+    int best_l = b->lanes, best_cl = 0;
+    for (int cl : {16, 8}) {
+        TRY(apply_cluster(cl));
+        for (int L : {1, 2, 4, 8, 16, 32}) {
+            if (L > 1 && L / 2 >= most) break;
+            BatchGraph g;
+            TRY(capture_batch(b, f, n, L, &g));
+            float ms = 0.0f;
+            const int rc = time_graph(b, g.exec, 3, &ms);
+            cudaGraphExecDestroy(g.exec);
+            TRY(rc);
+            if (ms < best) {
+                best = ms;
+                best_l = L;
+                best_cl = cl;
+            }
         }
     }
+    TRY(apply_cluster(best_cl));
     b->lanes = best_l;
     if (best_ms) *best_ms = best;
     return ISAR_OK;

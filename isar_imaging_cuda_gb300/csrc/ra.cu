@@ -35,9 +35,10 @@ __device__ __forceinline__ float2 row_phase(int64_t hq, int64_t sq, int n)
 }
 
 // Twiddle table of the range-alignment kernels: the two-level shared table
-// above 2048 points.  (A full N-entry table is read with strides of 32 words
-// by the radix-16 passes, i.e. with many-way bank conflicts; the two-level
-// table's hi/lo lookups spread or broadcast across a warp.)
+// above 2048 points (1.5 KB at N = 8192, filled by every CTA).  Measured
+// alternatives were slower: a full N-entry table (read with 32-word strides
+// by the radix-16 passes: many-way bank conflicts) and one exact table per
+// pass (69 KB per CTA: the fill costs more than the saved multiplies).
 template <int N>
 using RaTw = TwShared<N>;
 
@@ -721,8 +722,12 @@ static size_t pair_smem()
 {
     return ((size_t)FFTShape<N>::SMEM + RaTw<N>::kEntries) * sizeof(float2) + 2 * N * sizeof(float);
 }
+// range-alignment row kernels: FFT scratch + pass twiddle tables
 template <int N>
-static size_t fft_smem() { return ((size_t)FFTShape<N>::SMEM + RaTw<N>::kEntries) * sizeof(float2); }
+static size_t ra_fft_smem() { return ((size_t)FFTShape<N>::SMEM + RaTw<N>::kEntries) * sizeof(float2); }
+// kernels on the global twiddle table: FFT scratch only
+template <int N>
+static size_t fft_smem() { return (size_t)FFTShape<N>::SMEM * sizeof(float2); }
 
 template <int N>
 static cudaError_t set_attrs()
@@ -733,9 +738,10 @@ static cudaError_t set_attrs()
     const int big = (int)pair_smem<N>();
     if ((e = cudaFuncSetAttribute(k_ra_pair<N>, cudaFuncAttributeMaxDynamicSharedMemorySize, big))) return e;
     if ((e = cudaFuncSetAttribute(k_ra_corr<N>, cudaFuncAttributeMaxDynamicSharedMemorySize, big))) return e;
+    const int r = (int)ra_fft_smem<N>();
+    if ((e = cudaFuncSetAttribute(k_ra_accum<N>, cudaFuncAttributeMaxDynamicSharedMemorySize, r))) return e;
+    if ((e = cudaFuncSetAttribute(k_ra_final<N>, cudaFuncAttributeMaxDynamicSharedMemorySize, r))) return e;
     const int f = (int)fft_smem<N>();
-    if ((e = cudaFuncSetAttribute(k_ra_accum<N>, cudaFuncAttributeMaxDynamicSharedMemorySize, f))) return e;
-    if ((e = cudaFuncSetAttribute(k_ra_final<N>, cudaFuncAttributeMaxDynamicSharedMemorySize, f))) return e;
     if ((e = cudaFuncSetAttribute(k_ifds_pre<N>, cudaFuncAttributeMaxDynamicSharedMemorySize, f))) return e;
     if ((e = cudaFuncSetAttribute(k_fft_rows<N, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, f))) return e;
     if ((e = cudaFuncSetAttribute(k_fft_rows<N, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, f))) return e;
@@ -776,7 +782,7 @@ static cudaError_t ra_run_n(const RAArgs& a, cudaStream_t st)
             if (rpc > s / 2) rpc = s / 2;
             const int nch = (s / 2) / rpc;
             const int groups = M / s;
-            k_ra_accum<N><<<groups * nch, T, fft_smem<N>(), st>>>(a.x, a.win, a.hq, a.SQ, lv, rpc, a.part, a.tw);
+            k_ra_accum<N><<<groups * nch, T, ra_fft_smem<N>(), st>>>(a.x, a.win, a.hq, a.SQ, lv, rpc, a.part, a.tw);
             ISAR_COUNT(1);
             float* E = bufs[cur];
             dim3 g((N + 255) / 256, groups);
@@ -797,7 +803,7 @@ static cudaError_t ra_run_n(const RAArgs& a, cudaStream_t st)
     const int arp_rows = M < 256 ? M : 256;
     int rpcf = a.rpc_final;
     while (rpcf > 1 && (M % rpcf)) rpcf >>= 1;
-    k_ra_final<N><<<M / rpcf, T, fft_smem<N>(), st>>>(a.x, a.y, a.win, a.hq, a.SQ, rpcf, arp_rows, a.part, a.hmax,
+    k_ra_final<N><<<M / rpcf, T, ra_fft_smem<N>(), st>>>(a.x, a.y, a.win, a.hq, a.SQ, rpcf, arp_rows, a.part, a.hmax,
                                                       a.tw);
     ISAR_COUNT(1);
     const int nparts = (arp_rows + rpcf - 1) / rpcf;
