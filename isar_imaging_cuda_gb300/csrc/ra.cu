@@ -34,6 +34,41 @@ __device__ __forceinline__ float2 row_phase(int64_t hq, int64_t sq, int n)
     return cis_frac64(ph);
 }
 
+// Row phase exp(j 2 pi (hq n^2 - sq n) / 2^64) of the 16 first-pass elements
+// n = lt + r N/16 of one thread, requested for r = 0..15 in order.  With
+// D = N/16 the fixed-point phase is exactly ph0 + r A + r^2 B
+// (A = 2 hq lt D - sq D, B = hq D^2), so consecutive elements differ by the
+// rotor cis(A + (2r+1) B), which itself turns by cis(2B).  Values are exact
+// (sincospif of the fixed-point phase) at r = 0 and r = 8 and advanced by
+// two complex multiplies in between: 5 sincospif per 16 elements instead of
+// 16, with at most 7 rotor steps (~1e-6 relative) of accumulated rounding.
+template <int N>
+struct RowPhase {
+    float2 C, S, Q;
+    uint64_t ph0, A, B;
+    __device__ __forceinline__ void init(int64_t hq, int64_t sq, int lt)
+    {
+        constexpr uint64_t D = N / 16;
+        const uint64_t j = (uint64_t)lt;
+        ph0 = (uint64_t)hq * (j * j) - (uint64_t)sq * j;
+        A = 2ull * (uint64_t)hq * j * D - (uint64_t)sq * D;
+        B = (uint64_t)hq * (D * D);
+        Q = cis_frac64(2ull * B);
+    }
+    __device__ __forceinline__ float2 at(int r)
+    {
+        if (r == 0 || r == 8) {
+            const uint64_t rr = (uint64_t)r;
+            C = cis_frac64(ph0 + rr * A + rr * rr * B);
+            S = cis_frac64(A + (2ull * rr + 1ull) * B);
+        } else {
+            C = cmul(C, S);
+            S = cmul(S, Q);
+        }
+        return C;
+    }
+};
+
 // Twiddle table of the range-alignment kernels: the two-level shared table
 // above 2048 points (1.5 KB at N = 8192, filled by every CTA).  Measured
 // alternatives were slower: a full N-entry table (read with 32-word strides
@@ -182,7 +217,8 @@ __device__ __forceinline__ float csum3(float hi, float lo, float x)
 // then evaluated directly, sum_n a[n] b[n - tau] with error-free float
 // accumulation, because the second difference of a broad correlation peak
 // magnifies FFT rounding into ~1e-4-cell shift errors.  ea, eb are adjacent
-// N-float shared arrays and stay intact; sm_f is the FFT scratch.
+// N-float shared arrays of squared envelopes; they are replaced in place by
+// the amplitudes a, b.  sm_f is the FFT scratch.
 template <int N, class Tw>
 __device__ float ra_correlate(float* ea, float* sm_f, int lt, const Tw& tw)
 {
@@ -194,8 +230,10 @@ __device__ float ra_correlate(float* ea, float* sm_f, int lt, const Tw& tw)
     __shared__ float2 redp[32];
     __shared__ float s_res;
     __shared__ int s_pos;
+    for (int i = lt; i < 2 * N; i += T) ea[i] = sqrtf(ea[i]);
+    __syncthreads();
     // z = a + i b, forward FFT, spectrum kept in the scratch (padded slots)
-    team_fft<N, false>([&](int i) { return make_float2(sqrtf(ea[i]), sqrtf(eb[i])); },
+    team_fft<N, false>([&](int i) { return make_float2(ea[i], eb[i]); },
                        [&](int i, float2 v, int) { sm[fpad(i)] = v; }, sm, lt, tw);
     // C[k] = A[k] * conj(B[k]) with A, B split from Z; corr = Re IFFT(C);
     // argmax over the ifftshifted index (i + N/2) mod N tracked per thread
@@ -228,9 +266,9 @@ __device__ float ra_correlate(float* ea, float* sm_f, int lt, const Tw& tw)
 #pragma unroll 4
     for (int t = 0; t < N / T; ++t) {
         const int n = lt + t * T;
-        const float a = sqrtf(ea[n]);
+        const float a = ea[n];
 #pragma unroll
-        for (int j = 0; j < 3; ++j) acc_prod(a, sqrtf(eb[(n - tau - (j - 1)) & (N - 1)]), h[j], l[j]);
+        for (int j = 0; j < 3; ++j) acc_prod(a, eb[(n - tau - (j - 1)) & (N - 1)], h[j], l[j]);
     }
     double f[3];
 #pragma unroll
@@ -267,10 +305,12 @@ __device__ __forceinline__ void ra_row_power(const float2* __restrict__ xr, cons
                                              const Tw& tw)
 {
     const float invN = 1.0f / (float)N;
+    RowPhase<N> rp;
+    rp.init(h, sq, lt);
     team_fft<N, true>(
-        [&](int i) {
+        [&](int i) {   // i = lt + r N/16, r = 0..15 in order
             const float2 v = xr[i];
-            return cscale(cmul(v, row_phase(h, sq, i)), __ldg(&win[i]));
+            return cscale(cmul(v, rp.at((i - lt) / (N / 16))), __ldg(&win[i]));
         },
         [&](int, float2 v, int slot) {
             const float re = v.x * invN, im = v.y * invN;
@@ -436,8 +476,10 @@ k_ra_final(const float2* x, float2* yout, const float* __restrict__ win, const i
         const float2* xr = x + (size_t)row * N;
         float2* yr = yout + (size_t)row * N;
         const bool arp = row < arp_rows;
+        RowPhase<N> rp;
+        rp.init(h, sq, lt);
         team_fft<N, true>(
-            [&](int i) { return cscale(cmul(xr[i], row_phase(h, sq, i)), __ldg(&win[i])); },
+            [&](int i) { return cscale(cmul(xr[i], rp.at((i - lt) / (N / 16))), __ldg(&win[i])); },
             [&](int i, float2 v, int slot) {
                 const float2 y = make_float2(v.x * invN, v.y * invN);
                 yr[i] = y;
