@@ -126,6 +126,15 @@ struct TwShared {
     }
 };
 
+template <class Tw>
+struct TwTwoLevel {
+    static constexpr bool value = false;
+};
+template <int N, bool F>
+struct TwTwoLevel<TwShared<N, F>> {
+    static constexpr bool value = TwShared<N, F>::kTwoLevel;
+};
+
 template <int N, int R, int NS, bool INV, bool FIRST, bool LAST, class Src, class Dst, class Tw>
 __device__ __forceinline__ void fft_pass(Src& src, Dst& dst, float2* sm, int lt, const Tw& tw, bool active)
 {
@@ -155,7 +164,28 @@ __device__ __forceinline__ void fft_pass(Src& src, Dst& dst, float2* sm, int lt,
         for (int b = 0; b < B; ++b) {
             const int j = lt + b * T;
             const int k = j & (NS - 1);
-            if constexpr (NS > 1) {
+            if constexpr (NS > 1 && R == 16 && TwTwoLevel<Tw>::value) {
+                // two-level table: look up W^k, W^2k, W^4k, W^8k and form the
+                // others as products (depth <= 3): 8 shared loads instead of 30
+                constexpr int s = N / (NS * R);
+                float2 w[16];
+                w[1] = tw(k * s, N);
+                w[2] = tw(2 * k * s, N);
+                w[4] = tw(4 * k * s, N);
+                w[8] = tw(8 * k * s, N);
+                w[3] = cmul(w[2], w[1]);
+                w[5] = cmul(w[4], w[1]);
+                w[6] = cmul(w[4], w[2]);
+                w[7] = cmul(w[4], w[3]);
+#pragma unroll
+                for (int r = 9; r < 16; ++r) w[r] = cmul(w[8], w[r - 8]);
+#pragma unroll
+                for (int r = 1; r < 16; ++r) {
+                    float2 x = w[r];
+                    if (INV) x.y = -x.y;
+                    v[b * R + r] = cmul(v[b * R + r], x);
+                }
+            } else if constexpr (NS > 1) {
 #pragma unroll
                 for (int r = 1; r < R; ++r) {
                     float2 w = tw((r * k) * (N / (NS * R)), N);
