@@ -452,12 +452,16 @@ k_af_persist(const float2* __restrict__ cut, const int* __restrict__ bins, const
 template <int M>
 struct AFC {
     static constexpr int T = M / 16;
-    static constexpr int TEAMS = 4096 / M;     // 256 threads per CTA (two FFTs need ~255 registers)
-    static constexpr int THREADS = TEAMS * T;
+    static constexpr int TEAMS = 4096 / M;     // 256 threads per CTA
+    static constexpr int THREADS = TEAMS * T;  // (two fused FFTs need ~255 registers: one CTA per SM)
     static constexpr int NSLOT = 4;            // cached columns per CTA: 16384 / M
-    static constexpr size_t SMEM_F2 = 2 * (size_t)M + (size_t)TEAMS * FFTShape<M>::SMEM + (size_t)NSLOT * TEAMS * M +
-                                      TwShared<M>::kEntries;
+    using Tw = TwShared<M, false, true>;       // two-level twiddles (80 entries at M = 1024)
+    // phase copy + FFT scratch (also holds P and the reduction buffer between
+    // sweeps) + column cache + twiddles: ~171 KB at M = 1024
+    static constexpr size_t SMEM_F2 =
+        (size_t)M + (size_t)TEAMS * FFTShape<M>::SMEM + (size_t)NSLOT * TEAMS * M + Tw::kEntries;
     static constexpr size_t SMEM = SMEM_F2 * sizeof(float2) + 64 * sizeof(double);
+    static constexpr int PR = (M + THREADS - 1) / THREADS;   // partial-sum rows per thread
 };
 
 struct AFFrame {
@@ -477,19 +481,20 @@ k_af_cluster(AFFrame f, int iters, float tol, const float2* __restrict__ tw)
     namespace cg = cooperative_groups;
     using A = AFC<M>;
     using F = FFTShape<M>;
+    using TwA = typename A::Tw;
     cg::cluster_group cl = cg::this_cluster();
     const int CL = (int)cl.num_blocks();
     const int r = (int)cl.block_rank();
     extern __shared__ float4 dyn_smem[];
     float2* ph = reinterpret_cast<float2*>(dyn_smem);   // [M]
-    float2* P = ph + M;                                  // [M]
-    float2* smb = P + M;                                 // [TEAMS][SMEM]
+    float2* smb = ph + M;                                // [TEAMS][SMEM]; between sweeps: P [M], buf
+    float2* P = smb;
     float2* cache = smb + A::TEAMS * F::SMEM;            // [NSLOT][TEAMS][M]
     float2* twt = cache + (size_t)A::NSLOT * A::TEAMS * M;   // twiddle table
-    double* red = reinterpret_cast<double*>(twt + TwShared<M>::kEntries);   // [64]
-    const TwShared<M> tws{twt};
+    double* red = reinterpret_cast<double*>(twt + TwA::kEntries);   // [64]
+    const TwA tws{twt};
     const int tid = threadIdx.x;
-    TwShared<M>::fill(twt, tw, tid, A::THREADS);
+    TwA::fill(twt, tw, tid, A::THREADS);
     const int team = tid / F::T, lt = tid % F::T;
     const int lane = tid & 31, warp = tid >> 5;
     const int U = f.fdec[1];
@@ -516,10 +521,13 @@ k_af_cluster(AFFrame f, int iters, float tol, const float2* __restrict__ tw)
     const int rows = M / CL;
 
     // One sweep over this CTA's bins with the phase in ph: entropy sums
-    // (s1, s2) and, when `full`, the partial row sums P of the update.
-    auto sweep = [&](bool full, float& s1, float& s2) {
-        if (full)
-            for (int m = tid; m < M; m += A::THREADS) P[m] = make_float2(0.0f, 0.0f);
+    // (s1, s2, only when `ent`) and, when `full`, the partial row sums of the
+    // update, accumulated in registers and left in P (the start of the FFT
+    // scratch) for the cluster reduction.
+    auto sweep = [&](bool full, bool ent, float& s1, float& s2) {
+        float2 pacc[A::PR];
+#pragma unroll
+        for (int k = 0; k < A::PR; ++k) pacc[k] = make_float2(0.0f, 0.0f);
 #pragma unroll 1
         for (int j = 0; j < nch; ++j) {
             const int slot = j < A::NSLOT ? j : A::NSLOT - 1;
@@ -533,8 +541,10 @@ k_af_cluster(AFFrame f, int iters, float tol, const float2* __restrict__ tw)
             team_fft<M, false>([&](int i) { return cmul(ph[i], g[i]); },
                                [&](int i, float2 v, int) {
                                    const float p = v.x * v.x + v.y * v.y;
-                                   s1 += p;
-                                   if (p > 0.0f) s2 += p * logf(p);
+                                   if (ent) {
+                                       s1 += p;
+                                       if (p > 0.0f) s2 += p * logf(p);
+                                   }
                                    sm[fpad(i)] = cscale(v, sqrtf(p));
                                },
                                sm, lt, tws, valid);
@@ -543,14 +553,23 @@ k_af_cluster(AFFrame f, int iters, float tol, const float2* __restrict__ tw)
                               [&](int i, float2 v, int) { sm[fpad(i)] = cmulc(g[i], cscale(v, invM)); }, sm, lt,
                               tws, valid);
             const int nt = min(A::TEAMS, nb - j * A::TEAMS);
-            for (int m = tid; m < M; m += A::THREADS) {
-                float2 s = P[m];
-                for (int t = 0; t < nt; ++t) {
-                    const float2 q = smb[t * F::SMEM + fpad(m)];
-                    s.x += q.x;
-                    s.y += q.y;
-                }
-                P[m] = s;
+#pragma unroll
+            for (int k = 0; k < A::PR; ++k) {
+                const int m = tid + k * A::THREADS;
+                if (m < M)
+                    for (int t = 0; t < nt; ++t) {
+                        const float2 q = smb[t * F::SMEM + fpad(m)];
+                        pacc[k].x += q.x;
+                        pacc[k].y += q.y;
+                    }
+            }
+        }
+        if (full) {
+            __syncthreads();   // every team is done with the scratch
+#pragma unroll
+            for (int k = 0; k < A::PR; ++k) {
+                const int m = tid + k * A::THREADS;
+                if (m < M) P[m] = pacc[k];
             }
         }
     };
@@ -566,7 +585,7 @@ k_af_cluster(AFFrame f, int iters, float tol, const float2* __restrict__ tw)
                 for (int m = tid; m < M; m += A::THREADS) ph[m] = f.alt[m];
             }
             float s1 = 0.0f, s2 = 0.0f;
-            sweep(false, s1, s2);
+            sweep(false, true, s1, s2);
 #pragma unroll
             for (int o = 16; o > 0; o >>= 1) {
                 s1 += __shfl_xor_sync(0xffffffffu, s1, o);
@@ -616,8 +635,11 @@ k_af_cluster(AFFrame f, int iters, float tol, const float2* __restrict__ tw)
     int used = iters;
 #pragma unroll 1
     for (int it = 0; it < iters; ++it) {
+        // the entropy is needed by the stop criterion, and for the trace at
+        // the last iteration; elsewhere its logarithms are skipped
+        const bool need_e = tol > 0.0f || it == iters - 1;
         float s1 = 0.0f, s2 = 0.0f;
-        sweep(true, s1, s2);
+        sweep(true, need_e, s1, s2);
         // Entropy sums: float per warp, double per CTA (red[32..33]) and per
         // cluster, all by one thread (FP64 is slow on this part).
 #pragma unroll
@@ -647,14 +669,17 @@ k_af_cluster(AFFrame f, int iters, float tol, const float2* __restrict__ tw)
                 S1 += rr[32];
                 S2 += rr[33];
             }
-            const float E = logf((float)S1) - (float)S2 / (float)S1;
-            const bool stop = tol > 0.0f && it > 0 && fabsf(E - e_prev) <= tol * fabsf(E);
-            e_prev = E;
+            bool stop = false;
+            if (need_e) {
+                const float E = logf((float)S1) - (float)S2 / (float)S1;
+                stop = tol > 0.0f && it > 0 && fabsf(E - e_prev) <= tol * fabsf(E);
+                e_prev = E;
+            }
             red[40] = stop ? 1.0 : 0.0;
         }
         // This CTA's rows [r*rows, (r+1)*rows) of every CTA's partial sums,
-        // gathered with independent remote loads into buf[q][row].
-        float2* buf = smb;
+        // gathered with independent remote loads into buf[q][row] (behind P).
+        float2* buf = smb + M;
         for (int idx = tid; idx < CL * rows; idx += A::THREADS) {
             const int q = idx / rows, ml = idx - q * rows;
             buf[idx] = cl.map_shared_rank(P, q)[r * rows + ml];

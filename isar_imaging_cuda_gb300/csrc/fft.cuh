@@ -97,11 +97,12 @@ struct TwGlobal {
 };
 
 // TwShared<N>: a per-CTA shared-memory table.  For N <= 2048 (or FULL) it
-// holds all N twiddles; above that a two-level table hi[e >> 6] * lo[e & 63]
-// (N/64 + 64 entries, one extra complex multiply, ~1 ulp more rounding).
-template <int N, bool FULL = false>
+// holds all N twiddles; above that (or with TWO) a two-level table
+// hi[e >> 6] * lo[e & 63] (N/64 + 64 entries, one extra complex multiply,
+// ~1 ulp more rounding).
+template <int N, bool FULL = false, bool TWO = false>
 struct TwShared {
-    static constexpr bool kTwoLevel = !FULL && N > 2048;
+    static constexpr bool kTwoLevel = TWO || (!FULL && N > 2048);
     static constexpr int kEntries = kTwoLevel ? N / 64 + 64 : N;
     const float2* p;
     __device__ __forceinline__ float2 operator()(int e, int) const
@@ -130,9 +131,9 @@ template <class Tw>
 struct TwTwoLevel {
     static constexpr bool value = false;
 };
-template <int N, bool F>
-struct TwTwoLevel<TwShared<N, F>> {
-    static constexpr bool value = TwShared<N, F>::kTwoLevel;
+template <int N, bool F, bool T>
+struct TwTwoLevel<TwShared<N, F, T>> {
+    static constexpr bool value = TwShared<N, F, T>::kTwoLevel;
 };
 
 template <int N, int R, int NS, bool INV, bool FIRST, bool LAST, class Src, class Dst, class Tw>
