@@ -40,10 +40,10 @@ TOL = 1e-6                  # autofocus entropy stop criterion of the headline
 METRIC = "frames/s @1024×8192 c64: learned+batched vs plain on 1 GB300, equal entropy"
 WORKLOAD = ("full five-stage pipeline, 1024 pulses x 8192 range cells complex64, HPC + MTRC on, "
             "batches of 32 frames")
-# DRAM bytes per launch of the level-0 range-alignment kernel (k_ra_pair<8192>,
-# 512 pairs) from the ncu capture summarised in
-# profiles/range_alignment_1024x8192.md
-RA_PAIR_L0_TRAFFIC = None
+# DRAM bytes (read + write) of one range-alignment stage at 1024 x 8192, all
+# its kernels, from the ncu capture summarised in
+# profiles/range_alignment_1024x8192_dram.md
+RA_STAGE_TRAFFIC = 530624256
 
 
 def dist_init():
@@ -309,7 +309,7 @@ def run_gb300(args):
                       "HPC fused), single frame", "bound": "hbm",
             "achieved": ra_bytes / (stage_ms["range_align"] * 1e-3) / 1e9, "algorithmic_bytes": ra_bytes,
             "ms": stage_ms["range_align"], "peak": peak, "unit": "GB/s", "peak_kind": peak_kind,
-            "traffic": RA_PAIR_L0_TRAFFIC}
+            "traffic": RA_STAGE_TRAFFIC}
     roof["frac"] = roof["achieved"] / peak
 
     out = {
