@@ -339,12 +339,81 @@ def run_gb300(args):
         "gpu_launches": int(launches),
         "clocks": clk,
     }
-    if rank == 0 and not args.no_cpu:
-        out["cpu_baseline"] = cpu_baseline(X[0], V[0])
     batch.close()
     net.close()
+    if rank == 0 and not args.no_cpu:
+        out["cpu_baseline"] = cpu_baseline(X[0], V[0])
+    if rank == 0:
+        del X, X2, V2, imgs, imgs2, HX
+        torch.cuda.empty_cache()
+        out["other_workloads"] = other_workloads(g, torch, s, args.steps)
     if rank == 0:
         print(json.dumps(out))
+
+
+def other_workloads(g, torch, s, steps):
+    """The other configurations: the plain 256 x 4096 workload (single frame
+    per call, and batches of 32 frames), and 64 frames of uneven size
+    (pulses uniform over {128, 256, 512, 1024}, range cells over
+    {2048, 4096, 8192}, plain-workload scenes) in one batch graph."""
+    import numpy as np
+
+    def timed(fn, reps):
+        for _ in range(2):
+            fn()
+        s.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(s)
+        for _ in range(reps):
+            fn()
+        e1.record(s)
+        s.synchronize()
+        return e0.elapsed_time(e1) / reps
+
+    out = {}
+    # plain workload, 256 pulses x 4096 range cells, no HPC / MTRC
+    m1, n1, b1 = 256, 4096, 32
+    rp1 = g.radar(m1, n1)
+    X = torch.empty((b1, m1, 2 * n1), dtype=torch.float32, device="cuda")
+    img = torch.empty((b1, m1, C), dtype=torch.float32, device="cuda")
+    for i in range(b1):
+        g.synth_device(g.synth_params(m1, n1, seed=5000 + i), X[i], None, s.cuda_stream)
+    with g.Context(rp1, stream=s.cuda_stream) as ctx:
+        k = [0]
+
+        def one():
+            ctx.image_device(X[k[0] % b1], None, img[k[0] % b1], 0)
+            k[0] += 1
+        ms1 = timed(one, max(steps, 10))
+    with g.Batch(stream=s.cuda_stream) as b:
+        lst = g.Batch.frames((rp1, X[i], None, 0, img[i]) for i in range(b1))
+        b.autotune(lst)
+        msb = timed(lambda: b.run(lst), max(steps // 2, 3))
+        lanes = b.lanes()
+    out["plain_256x4096"] = {"single_frame_frames_per_s": 1e3 / ms1, "batch32_frames_per_s": b1 * 1e3 / msb,
+                             "batch_lanes": lanes}
+    del X, img
+    # 64 frames of uneven size in one batch graph
+    rng = np.random.default_rng(2024)
+    Ms = rng.choice([128, 256, 512, 1024], 64)
+    Ns = rng.choice([2048, 4096, 8192], 64)
+    frames, keep = [], []
+    for i, (m, n) in enumerate(zip(Ms, Ns)):
+        m, n = int(m), int(min(max(n, m), 8192))
+        x = torch.empty((m, 2 * n), dtype=torch.float32, device="cuda")
+        im = torch.empty((m, C), dtype=torch.float32, device="cuda")
+        g.synth_device(g.synth_params(m, n, seed=7000 + i), x, None, s.cuda_stream)
+        keep += [x, im]
+        frames.append((g.radar(m, n), x, None, 0, im))
+    with g.Batch(stream=s.cuda_stream) as b:
+        lst = g.Batch.frames(frames)
+        b.autotune(lst)
+        msu = timed(lambda: b.run(lst), max(steps // 2, 3))
+        lanes = b.lanes()
+    out["uneven_batch64"] = {"frames_per_s": 64 * 1e3 / msu, "ms_per_batch": msu, "lanes_per_shape": lanes,
+                             "shapes": len({(int(a), int(c)) for a, c in zip(Ms, Ns)}),
+                             "pulse_cells": int(sum(int(a) * int(c) for a, c in zip(Ms, Ns)))}
+    return out
 
 
 def cpu_baseline(frame, vel):
