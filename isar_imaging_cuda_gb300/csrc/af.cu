@@ -716,6 +716,237 @@ k_af_cluster(AFFrame f, int iters, float tol, const float2* __restrict__ tw)
     }
 }
 
+// ---------------------------------------------------------------------------
+// k_af_cluster for M = 1024 on warp-level FFTs (warp_fft1024): one warp per
+// bin, 8 bins per round per CTA.  Element m of a bin lives in lane m % 32,
+// register m / 32 through the forward transform, the T |T| epilogue and the
+// inverse transform (conj-forward-conj), with no shared-memory round trip
+// and no block barrier between them.  Per-warp partial row sums accumulate
+// in registers across rounds and are reduced over the CTA's warps in fixed
+// order; the cluster reduction, stop criterion and the choice of start are
+// those of k_af_cluster.
+// ---------------------------------------------------------------------------
+struct AFW {
+    static constexpr int M = 1024;
+    static constexpr int WARPS = 8;
+    static constexpr int THREADS = WARPS * 32;
+    static constexpr int TILE = 32 * 33;       // per-warp transpose tile (float2)
+    static constexpr int NSLOT = 2;            // cached rounds: 16 bins per CTA
+    static constexpr size_t SMEM_F2 = (size_t)M + (size_t)WARPS * TILE + (size_t)NSLOT * WARPS * M + M;
+    static constexpr size_t SMEM = SMEM_F2 * sizeof(float2) + 64 * sizeof(double);
+};
+
+__global__ void __launch_bounds__(AFW::THREADS, 1)
+k_af_cluster_w1024(AFFrame f, int iters, float tol, const float2* __restrict__ tw)
+{
+    namespace cg = cooperative_groups;
+    constexpr int M = AFW::M;
+    cg::cluster_group cl = cg::this_cluster();
+    const int CL = (int)cl.num_blocks();
+    const int r = (int)cl.block_rank();
+    extern __shared__ float4 dyn_smem[];
+    float2* ph = reinterpret_cast<float2*>(dyn_smem);          // [M]
+    float2* tiles = ph + M;                                     // [WARPS][TILE]; between sweeps P, buf
+    float2* cache = tiles + AFW::WARPS * AFW::TILE;             // [NSLOT][WARPS][M]
+    float2* T = cache + (size_t)AFW::NSLOT * AFW::WARPS * M;    // W_1024^i
+    double* red = reinterpret_cast<double*>(T + M);             // [64]
+    float2* P = tiles;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    for (int i = tid; i < M; i += AFW::THREADS) T[i] = tw[i * (kTwN / M)];
+    float2* tile = tiles + warp * AFW::TILE;
+    const int U = f.fdec[1];
+    const int bpc = (U + CL - 1) / CL;
+    const int b0 = r * bpc;
+    const int nb = max(0, min(bpc, U - b0));
+    const int nrd = (nb + AFW::WARPS - 1) / AFW::WARPS;
+    const bool reload = nrd > AFW::NSLOT;
+
+    auto load_col = [&](int j, int slot) {   // this warp's bin of round j into slot
+        const int t = j * AFW::WARPS + warp;
+        float2* g = cache + ((size_t)slot * AFW::WARPS + warp) * M;
+        if (t < nb) {
+            const int b = f.bins[b0 + t];
+            for (int m = lane; m < M; m += 32) g[m] = f.cut[(size_t)m * C + b];
+        }
+    };
+    for (int m = tid; m < M; m += AFW::THREADS) ph[m] = f.phase[m];
+    for (int j = 0; j < min(nrd, AFW::NSLOT); ++j) load_col(j, j);
+    __syncthreads();
+
+    const float invM = 1.0f / (float)M;
+    const int rows = M / CL;
+
+    // One sweep with the phase in ph; see k_af_cluster.
+    auto sweep = [&](bool full, bool ent, float& s1, float& s2) {
+        float2 pacc[32];
+#pragma unroll
+        for (int k = 0; k < 32; ++k) pacc[k] = make_float2(0.0f, 0.0f);
+#pragma unroll 1
+        for (int j = 0; j < nrd; ++j) {
+            const int slot = j < AFW::NSLOT ? j : AFW::NSLOT - 1;
+            if (j * AFW::WARPS + warp >= nb) continue;   // warp-uniform; no block barrier inside
+            if (reload && j >= AFW::NSLOT - 1) {
+                load_col(j, slot);
+                __syncwarp();
+            }
+            const float2* g = cache + ((size_t)slot * AFW::WARPS + warp) * M;
+            float2 v[32];
+#pragma unroll
+            for (int k = 0; k < 32; ++k) v[k] = cmul(ph[lane + 32 * k], g[lane + 32 * k]);
+            warp_fft1024(v, lane, tile, T);
+#pragma unroll
+            for (int k = 0; k < 32; ++k) {
+                const float p = v[k].x * v[k].x + v[k].y * v[k].y;
+                if (ent) {
+                    s1 += p;
+                    if (p > 0.0f) s2 += p * logf(p);
+                }
+                const float a = sqrtf(p);
+                v[k] = make_float2(v[k].x * a, -v[k].y * a);   // conj(T |T|)
+            }
+            if (!full) continue;
+            warp_fft1024(v, lane, tile, T);   // conj of IFFT(T |T|) * M
+#pragma unroll
+            for (int k = 0; k < 32; ++k) {
+                const float2 h = make_float2(v[k].x * invM, -v[k].y * invM);
+                const float2 q = cmulc(g[lane + 32 * k], h);
+                pacc[k].x += q.x;
+                pacc[k].y += q.y;
+            }
+            __syncwarp();   // slot reuse by the next reload
+        }
+        if (full) {
+            __syncthreads();   // every warp is done with its tile
+#pragma unroll
+            for (int k = 0; k < 32; ++k) tile[lane + 32 * k] = pacc[k];
+            __syncthreads();
+            for (int m = tid; m < M; m += AFW::THREADS) {
+                float2 s = tiles[m];
+#pragma unroll
+                for (int w = 1; w < AFW::WARPS; ++w) {
+                    const float2 q = tiles[w * AFW::TILE + m];
+                    s.x += q.x;
+                    s.y += q.y;
+                }
+                P[m] = s;
+            }
+        }
+    };
+
+    auto cluster_entropy = [&](float s1, float s2, double* slot) {
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            s1 += __shfl_xor_sync(0xffffffffu, s1, o);
+            s2 += __shfl_xor_sync(0xffffffffu, s2, o);
+        }
+        if (lane == 0) {
+            red[warp] = s1;
+            red[16 + warp] = s2;
+        }
+        __syncthreads();
+        if (tid == 0) {
+            double a1 = 0.0, a2 = 0.0;
+            for (int w = 0; w < AFW::WARPS; ++w) {
+                a1 += red[w];
+                a2 += red[16 + w];
+            }
+            red[32] = a1;
+            red[33] = a2;
+        }
+        cl.sync();
+        if (tid == 0) {
+            double S1 = 0.0, S2 = 0.0;
+            for (int q = 0; q < CL; ++q) {
+                const double* rr = cl.map_shared_rank(red, q);
+                S1 += rr[32];
+                S2 += rr[33];
+            }
+            *slot = logf((float)S1) - (float)S2 / (float)S1;
+        }
+    };
+
+    if (f.alt) {
+        float e_start[2];
+#pragma unroll 1
+        for (int k = 0; k < 2; ++k) {
+            if (k == 1) {
+                __syncthreads();
+                for (int m = tid; m < M; m += AFW::THREADS) ph[m] = f.alt[m];
+                __syncthreads();
+            }
+            float s1 = 0.0f, s2 = 0.0f;
+            sweep(false, true, s1, s2);
+            cluster_entropy(s1, s2, &red[41 + k]);
+            cl.sync();
+            e_start[k] = (float)red[41 + k];
+        }
+        const bool use_alt = e_start[1] < e_start[0];
+        if (!use_alt) {
+            __syncthreads();
+            for (int m = tid; m < M; m += AFW::THREADS) ph[m] = f.phase[m];
+        }
+        if (r == 0 && tid == 0 && f.stat) {
+            f.stat[2] = use_alt ? 1 : 0;
+            f.stat[3] = __float_as_int(e_start[0]);
+            f.stat[4] = __float_as_int(e_start[1]);
+        }
+        __syncthreads();
+    }
+
+    float e_prev = 0.0f;   // meaningful in thread 0
+    int used = iters;
+#pragma unroll 1
+    for (int it = 0; it < iters; ++it) {
+        const bool need_e = tol > 0.0f || it == iters - 1;
+        float s1 = 0.0f, s2 = 0.0f;
+        sweep(true, need_e, s1, s2);
+        cluster_entropy(s1, s2, &red[44]);
+        if (tid == 0) {
+            bool stop = false;
+            if (need_e) {
+                const float E = (float)red[44];
+                stop = tol > 0.0f && it > 0 && fabsf(E - e_prev) <= tol * fabsf(E);
+                e_prev = E;
+            }
+            red[40] = stop ? 1.0 : 0.0;
+        }
+        float2* buf = tiles + AFW::TILE;   // behind P (tile 0 holds P)
+        for (int idx = tid; idx < CL * rows; idx += AFW::THREADS) {
+            const int q = idx / rows, ml = idx - q * rows;
+            buf[idx] = cl.map_shared_rank(P, q)[r * rows + ml];
+        }
+        __syncthreads();
+        const bool stop = red[40] != 0.0;
+        if (!stop) {
+            for (int ml = tid; ml < rows; ml += AFW::THREADS) {
+                float2 s = make_float2(0.0f, 0.0f);
+                for (int q = 0; q < CL; ++q) {
+                    const float2 v = buf[q * rows + ml];
+                    s.x += v.x;
+                    s.y += v.y;
+                }
+                const float a = sqrtf(s.x * s.x + s.y * s.y);
+                buf[CL * rows + ml] = make_float2(s.x / a, s.y / a);
+            }
+            __syncthreads();
+            for (int idx = tid; idx < CL * rows; idx += AFW::THREADS) {
+                const int q = idx / rows, ml = idx - q * rows;
+                cl.map_shared_rank(ph, q)[r * rows + ml] = buf[CL * rows + ml];
+            }
+        }
+        cl.sync();
+        if (stop) {
+            used = it;
+            break;
+        }
+    }
+    for (int m = r * rows + tid; m < (r + 1) * rows; m += AFW::THREADS) f.phase[m] = ph[m];
+    if (r == 0 && tid == 0 && f.stat) {
+        f.stat[0] = used;
+        f.stat[1] = __float_as_int(e_prev);
+    }
+}
+
 // cut[m][c] *= phase[m]  (phase_adjustment.cu:324)
 __global__ void k_af_apply(float2* __restrict__ cut, const float2* __restrict__ phase, int M)
 {
@@ -730,6 +961,21 @@ __global__ void k_af_apply(float2* __restrict__ cut, const float2* __restrict__ 
 template <int M>
 static constexpr int af_cb() { return M >= 512 ? 8 : (M >= 256 ? 16 : 32); }
 
+// The cluster engine's kernel for M pulses: warp-level FFTs at M = 1024,
+// team FFTs otherwise.
+template <int M>
+struct AfEngine {
+    static constexpr bool kWarp = M == 1024;
+    static constexpr int THREADS = kWarp ? AFW::THREADS : AFC<M>::THREADS;
+    static constexpr size_t SMEM = kWarp ? AFW::SMEM : AFC<M>::SMEM;
+    using Fn = void (*)(AFFrame, int, float, const float2*);
+    static Fn kernel()
+    {
+        if constexpr (kWarp) return k_af_cluster_w1024;
+        else return k_af_cluster<M>;
+    }
+};
+
 // Cluster engine set-up (once per process): shared-memory limit, non-portable
 // cluster sizes, and the largest of 16/8/4 CTAs per cluster that can be
 // resident.  Returns that size, 0 if none, or a negative cudaError_t.
@@ -738,11 +984,11 @@ static int af_cluster_setup()
 {
     static int max_cl = -1;
     if (max_cl >= 0) return max_cl;
-    using A = AFC<M>;
+    using A = AfEngine<M>;
     cudaError_t e;
-    if ((e = cudaFuncSetAttribute(k_af_cluster<M>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)A::SMEM)))
+    if ((e = cudaFuncSetAttribute(A::kernel(), cudaFuncAttributeMaxDynamicSharedMemorySize, (int)A::SMEM)))
         return -(int)e;
-    if ((e = cudaFuncSetAttribute(k_af_cluster<M>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1))) {
+    if ((e = cudaFuncSetAttribute(A::kernel(), cudaFuncAttributeNonPortableClusterSizeAllowed, 1))) {
         (void)cudaGetLastError();
     }
     int best = 0;
@@ -759,7 +1005,7 @@ static int af_cluster_setup()
         cfg.attrs = at;
         cfg.numAttrs = 1;
         int n = 0;
-        if (cudaOccupancyMaxActiveClusters(&n, k_af_cluster<M>, &cfg) == cudaSuccess && n > 0) best = cl;
+        if (cudaOccupancyMaxActiveClusters(&n, A::kernel(), &cfg) == cudaSuccess && n > 0) best = cl;
         (void)cudaGetLastError();
     }
     max_cl = best;
@@ -769,7 +1015,7 @@ static int af_cluster_setup()
 template <int M>
 static cudaError_t af_cluster_launch(const FEArgs& a, cudaStream_t st)
 {
-    using A = AFC<M>;
+    using A = AfEngine<M>;
     const int mx = af_cluster_setup<M>();
     if (mx < 0) return (cudaError_t)(-mx);
     const int cl = a.af_cluster;
@@ -788,7 +1034,7 @@ static cudaError_t af_cluster_launch(const FEArgs& a, cudaStream_t st)
     cfg.attrs = at;
     cfg.numAttrs = 1;
     AFFrame fr{a.cut, a.bins, a.fdec, a.phase, a.af_stat, a.ws_w ? a.ws_phase : nullptr};
-    cudaError_t e = cudaLaunchKernelEx(&cfg, k_af_cluster<M>, fr, a.iters, a.tol, a.tw);
+    cudaError_t e = cudaLaunchKernelEx(&cfg, A::kernel(), fr, a.iters, a.tol, a.tw);
     if (e == cudaSuccess) ISAR_COUNT(1);
     return e;
 }

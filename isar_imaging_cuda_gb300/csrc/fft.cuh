@@ -251,4 +251,66 @@ __device__ __forceinline__ int fft_out_index(int lt, int slot)
     return lt + b * S::T + r * (N / R);
 }
 
+// ---------------------------------------------------------------------------
+// Warp-level 1024-point FFT (forward, unnormalised).  Lane l holds element
+// l + 32 r in register r (r = 0..31), before and after the transform.
+// Four-step: a 32-point DFT over the registers, the twiddles W_1024^(l k),
+// a transpose of the warp's 32 x 32 block through a shared tile (row stride
+// 33, __syncwarp only), and a second 32-point DFT over the registers.  No
+// block barrier, so the warps of a CTA run their transforms independently.
+// ---------------------------------------------------------------------------
+
+// In-register 32-point forward DFT, natural order in and out:
+// X[k] = E[k] + W32^k O[k], X[k + 16] = E[k] - W32^k O[k] with E, O the
+// 16-point DFTs of the even and odd elements.
+__device__ __forceinline__ void dft32_reg(float2* a)
+{
+    const float c[16] = {1.000000000f,  0.980785280f,  0.923879533f,  0.831469612f, 0.707106781f,  0.555570233f,
+                         0.382683432f,  0.195090322f,  0.000000000f,  -0.195090322f, -0.382683432f, -0.555570233f,
+                         -0.707106781f, -0.831469612f, -0.923879533f, -0.980785280f};
+    const float s[16] = {0.000000000f, 0.195090322f, 0.382683432f, 0.555570233f, 0.707106781f, 0.831469612f,
+                         0.923879533f, 0.980785280f, 1.000000000f, 0.980785280f, 0.923879533f, 0.831469612f,
+                         0.707106781f, 0.555570233f, 0.382683432f, 0.195090322f};
+    float2 e[16], o[16];
+#pragma unroll
+    for (int i = 0; i < 16; ++i) {
+        e[i] = a[2 * i];
+        o[i] = a[2 * i + 1];
+    }
+    dft_reg<16, false>(e);
+    dft_reg<16, false>(o);
+#pragma unroll
+    for (int k = 0; k < 16; ++k) {
+        // o[k] * exp(-j 2 pi k / 32)
+        const float2 t = make_float2(o[k].x * c[k] + o[k].y * s[k], o[k].y * c[k] - o[k].x * s[k]);
+        a[k] = cadd(e[k], t);
+        a[k + 16] = csub(e[k], t);
+    }
+}
+
+// T: W_1024^i for i < 1024 (shared); tile: this warp's 32 x 33 float2.
+__device__ __forceinline__ void warp_fft1024(float2* v, int lane, float2* tile, const float2* T)
+{
+    dft32_reg(v);
+    // v[k] *= W_1024^(lane k): exact table values at k = 0, 8, 16, 24, then
+    // up to 7 steps of W_1024^lane
+    const float2 w = T[lane];
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+        float2 t = T[(lane * 8 * j) & 1023];
+#pragma unroll
+        for (int q = 0; q < 8; ++q) {
+            v[8 * j + q] = cmul(v[8 * j + q], t);
+            if (q < 7) t = cmul(t, w);
+        }
+    }
+#pragma unroll
+    for (int k = 0; k < 32; ++k) tile[lane * 33 + k] = v[k];
+    __syncwarp();
+#pragma unroll
+    for (int n = 0; n < 32; ++n) v[n] = tile[n * 33 + lane];
+    __syncwarp();
+    dft32_reg(v);
+}
+
 }  // namespace isar
