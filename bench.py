@@ -483,7 +483,8 @@ def run_reference(args):
 def run_profile(args):
     """Profiling workloads (no timing, no JSON): `plain` images one
     1024 x 8192 frame warmup + steps times; `batch` runs a batch of 8
-    frames through isar_batch_run (cluster autofocus, learned warm start)."""
+    frames through isar_batch_run (8-CTA cluster autofocus, learned warm
+    start)."""
     import torch
 
     import isar_imaging_cuda_gb300 as g
@@ -507,7 +508,7 @@ def run_profile(args):
         net.load_params(g.WARMSTART_WEIGHTS)
         with g.Batch(stream=s.cuda_stream, lanes=8) as b:
             b.set_warmstart(net)
-            b.set_tuning(rp, g.Tuning(ra_pair_min=128, ra_rows_per_cta=4, ra_rows_final=4, af_cluster=16,
+            b.set_tuning(rp, g.Tuning(ra_pair_min=128, ra_rows_per_cta=4, ra_rows_final=4, af_cluster=8,
                                       af_tol=TOL, af_iters=120, af_cluster_max=0))
             lst = g.Batch.frames((rp, X[i], V[i], flags, imgs[i]) for i in range(nb))
             for _ in range(args.warmup + args.steps):

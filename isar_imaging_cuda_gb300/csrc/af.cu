@@ -472,6 +472,7 @@ struct AFFrame {
     int* stat;             // [0] iterations applied, [1] entropy bits, [2] alt start used,
                            // [3], [4] entropy bits of the two starts; may be null
     const float2* alt;     // [M] second start phase (learned warm start) or null
+    float2* gcol;          // [U][M] scratch: contiguous copy of the bin columns
 };
 
 template <int M>
@@ -720,11 +721,11 @@ k_af_cluster(AFFrame f, int iters, float tol, const float2* __restrict__ tw)
 // k_af_cluster for M = 1024 on warp-level FFTs (warp_fft1024): one warp per
 // bin, 8 bins per round per CTA.  Element m of a bin lives in lane m % 32,
 // register m / 32 through the forward transform, the T |T| epilogue and the
-// inverse transform (conj-forward-conj), with no shared-memory round trip
-// and no block barrier between them.  Per-warp partial row sums accumulate
-// in registers across rounds and are reduced over the CTA's warps in fixed
-// order; the cluster reduction, stop criterion and the choice of start are
-// those of k_af_cluster.
+// inverse transform (conj-forward-conj); the transposes go through the
+// warp's own tile, so no block barrier sits inside a sweep.  Per-warp partial
+// row sums accumulate in registers across rounds and are reduced over the
+// CTA's warps in fixed order; the cluster reduction, stop criterion and the
+// choice of start are those of k_af_cluster.
 // ---------------------------------------------------------------------------
 struct AFW {
     static constexpr int M = 1024;
@@ -736,6 +737,11 @@ struct AFW {
     static constexpr size_t SMEM = SMEM_F2 * sizeof(float2) + 64 * sizeof(double);
 };
 
+// Each warp keeps NSLOT of its bins in shared memory; when the CTA has more,
+// the others are read from gcol, a contiguous copy of the
+// gathered columns ([U][M], written by the loading warp itself on entry), and
+// successive sweeps alternate direction so that the NSLOT rounds left in
+// shared memory by one sweep are the first of the next.
 __global__ void __launch_bounds__(AFW::THREADS, 1)
 k_af_cluster_w1024(AFFrame f, int iters, float tol, const float2* __restrict__ tw)
 {
@@ -748,11 +754,11 @@ k_af_cluster_w1024(AFFrame f, int iters, float tol, const float2* __restrict__ t
     float2* ph = reinterpret_cast<float2*>(dyn_smem);          // [M]
     float2* tiles = ph + M;                                     // [WARPS][TILE]; between sweeps P, buf
     float2* cache = tiles + AFW::WARPS * AFW::TILE;             // [NSLOT][WARPS][M]
-    float2* T = cache + (size_t)AFW::NSLOT * AFW::WARPS * M;    // W_1024^i
-    double* red = reinterpret_cast<double*>(T + M);             // [64]
+    float2* TWL = cache + (size_t)AFW::NSLOT * AFW::WARPS * M;  // [32][32] W^(lane k)
+    double* red = reinterpret_cast<double*>(TWL + M);           // [64]
     float2* P = tiles;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    for (int i = tid; i < M; i += AFW::THREADS) T[i] = tw[i * (kTwN / M)];
+    for (int i = tid; i < M; i += AFW::THREADS) TWL[i] = tw[(i >> 5) * (i & 31) * (kTwN / M)];
     float2* tile = tiles + warp * AFW::TILE;
     const int U = f.fdec[1];
     const int bpc = (U + CL - 1) / CL;
@@ -760,65 +766,85 @@ k_af_cluster_w1024(AFFrame f, int iters, float tol, const float2* __restrict__ t
     const int nb = max(0, min(bpc, U - b0));
     const int nrd = (nb + AFW::WARPS - 1) / AFW::WARPS;
     const bool reload = nrd > AFW::NSLOT;
+    float2* gw = f.gcol + (size_t)(b0 + warp) * M;   // this warp's bin of round 0
 
-    auto load_col = [&](int j, int slot) {   // this warp's bin of round j into slot
-        const int t = j * AFW::WARPS + warp;
-        float2* g = cache + ((size_t)slot * AFW::WARPS + warp) * M;
-        if (t < nb) {
-            const int b = f.bins[b0 + t];
-            for (int m = lane; m < M; m += 32) g[m] = f.cut[(size_t)m * C + b];
-        }
-    };
     for (int m = tid; m < M; m += AFW::THREADS) ph[m] = f.phase[m];
-    for (int j = 0; j < min(nrd, AFW::NSLOT); ++j) load_col(j, j);
+    // every bin of this warp: cached rounds into their slot, all rounds into
+    // gcol when some must be re-read
+    for (int j = 0; j < nrd; ++j) {
+        const int t = j * AFW::WARPS + warp;
+        if (t >= nb || (j >= AFW::NSLOT && !reload)) continue;
+        const int b = f.bins[b0 + t];
+        float2* g = cache + ((size_t)(j % AFW::NSLOT) * AFW::WARPS + warp) * M;
+        float2* gg = gw + (size_t)j * AFW::WARPS * M;
+        for (int m = lane; m < M; m += 32) {
+            const float2 x = f.cut[(size_t)m * C + b];
+            if (j < AFW::NSLOT) g[m] = x;
+            if (reload) gg[m] = x;
+        }
+    }
     __syncthreads();
 
     const float invM = 1.0f / (float)M;
     const int rows = M / CL;
+    int nsweep = 0;
 
     // One sweep with the phase in ph; see k_af_cluster.
     auto sweep = [&](bool full, bool ent, float& s1, float& s2) {
         float2 pacc[32];
 #pragma unroll
         for (int k = 0; k < 32; ++k) pacc[k] = make_float2(0.0f, 0.0f);
+        const bool back = (nsweep++ & 1) != 0;
 #pragma unroll 1
-        for (int j = 0; j < nrd; ++j) {
-            const int slot = j < AFW::NSLOT ? j : AFW::NSLOT - 1;
+        for (int jj = 0; jj < nrd; ++jj) {
+            const int j = back ? nrd - 1 - jj : jj;
             if (j * AFW::WARPS + warp >= nb) continue;   // warp-uniform; no block barrier inside
-            if (reload && j >= AFW::NSLOT - 1) {
-                load_col(j, slot);
+            float2* g = cache + ((size_t)(j % AFW::NSLOT) * AFW::WARPS + warp) * M;
+            if (jj >= AFW::NSLOT) {   // only when reload: read the copy in gcol
+                const float4* src = reinterpret_cast<const float4*>(gw + (size_t)j * AFW::WARPS * M);
+                float4* dst = reinterpret_cast<float4*>(g);
+#pragma unroll 4
+                for (int i = lane; i < M / 2; i += 32) dst[i] = src[i];
                 __syncwarp();
             }
-            const float2* g = cache + ((size_t)slot * AFW::WARPS + warp) * M;
             float2 v[32];
 #pragma unroll
             for (int k = 0; k < 32; ++k) v[k] = cmul(ph[lane + 32 * k], g[lane + 32 * k]);
-            warp_fft1024(v, lane, tile, T);
+            // pass 0: T = FFT(phase * g); pass 1: conj(IFFT(T |T|)) * M as the
+            // forward FFT of conj(T |T|).  One copy of the transform's code
+            // (a loop, not unrolled) keeps the kernel within the instruction
+            // cache.
+#pragma unroll 1
+            for (int pass = 0; pass < (full ? 2 : 1); ++pass) {
+                warp_fft1024(v, lane, tile, TWL);
+                if (pass == 0) {
 #pragma unroll
-            for (int k = 0; k < 32; ++k) {
-                const float p = v[k].x * v[k].x + v[k].y * v[k].y;
-                if (ent) {
-                    s1 += p;
-                    if (p > 0.0f) s2 += p * logf(p);
+                    for (int k = 0; k < 32; ++k) {
+                        const float p = v[k].x * v[k].x + v[k].y * v[k].y;
+                        if (ent) {
+                            s1 += p;
+                            if (p > 0.0f) s2 += p * logf(p);
+                        }
+                        const float a = p > 0.0f ? p * rsqrtf(p) : 0.0f;
+                        v[k] = make_float2(v[k].x * a, -v[k].y * a);   // conj(T |T|)
+                    }
+                } else {
+                    // conj(g) conj(v) / M = conj(g v) / M: g v accumulates
+                    // here, the conjugate and 1/M are applied once per sweep
+#pragma unroll
+                    for (int k = 0; k < 32; ++k) {
+                        const float2 q = g[lane + 32 * k];
+                        pacc[k].x = fmaf(q.x, v[k].x, fmaf(-q.y, v[k].y, pacc[k].x));
+                        pacc[k].y = fmaf(q.x, v[k].y, fmaf(q.y, v[k].x, pacc[k].y));
+                    }
                 }
-                const float a = sqrtf(p);
-                v[k] = make_float2(v[k].x * a, -v[k].y * a);   // conj(T |T|)
             }
-            if (!full) continue;
-            warp_fft1024(v, lane, tile, T);   // conj of IFFT(T |T|) * M
-#pragma unroll
-            for (int k = 0; k < 32; ++k) {
-                const float2 h = make_float2(v[k].x * invM, -v[k].y * invM);
-                const float2 q = cmulc(g[lane + 32 * k], h);
-                pacc[k].x += q.x;
-                pacc[k].y += q.y;
-            }
-            __syncwarp();   // slot reuse by the next reload
+            __syncwarp();   // slot reuse by a later reload
         }
         if (full) {
             __syncthreads();   // every warp is done with its tile
 #pragma unroll
-            for (int k = 0; k < 32; ++k) tile[lane + 32 * k] = pacc[k];
+            for (int k = 0; k < 32; ++k) tile[lane + 32 * k] = make_float2(pacc[k].x * invM, -pacc[k].y * invM);
             __syncthreads();
             for (int m = tid; m < M; m += AFW::THREADS) {
                 float2 s = tiles[m];
@@ -1033,7 +1059,7 @@ static cudaError_t af_cluster_launch(const FEArgs& a, cudaStream_t st)
     cfg.stream = st;
     cfg.attrs = at;
     cfg.numAttrs = 1;
-    AFFrame fr{a.cut, a.bins, a.fdec, a.phase, a.af_stat, a.ws_w ? a.ws_phase : nullptr};
+    AFFrame fr{a.cut, a.bins, a.fdec, a.phase, a.af_stat, a.ws_w ? a.ws_phase : nullptr, a.gcol};
     cudaError_t e = cudaLaunchKernelEx(&cfg, A::kernel(), fr, a.iters, a.tol, a.tw);
     if (e == cudaSuccess) ISAR_COUNT(1);
     return e;

@@ -288,29 +288,25 @@ __device__ __forceinline__ void dft32_reg(float2* a)
     }
 }
 
-// T: W_1024^i for i < 1024 (shared); tile: this warp's 32 x 33 float2.
-__device__ __forceinline__ void warp_fft1024(float2* v, int lane, float2* tile, const float2* T)
+// TWL: W_1024^(l k) at TWL[32 k + l] (l, k < 32) in shared memory, read
+// lane-contiguous (conflict-free); tile: this warp's 32 x 33 float2.
+// v[k] holds x[lane + 32 k] on entry and X[lane + 32 k] on return.
+__device__ __forceinline__ void warp_fft1024(float2* v, int lane, float2* tile, const float2* TWL)
 {
-    dft32_reg(v);
-    // v[k] *= W_1024^(lane k): exact table values at k = 0, 8, 16, 24, then
-    // up to 7 steps of W_1024^lane
-    const float2 w = T[lane];
+    // two 32-point DFT steps sharing one copy of the code
+#pragma unroll 1
+    for (int step = 0; step < 2; ++step) {
+        dft32_reg(v);
+        if (step == 1) break;
 #pragma unroll
-    for (int j = 0; j < 4; ++j) {
-        float2 t = T[(lane * 8 * j) & 1023];
+        for (int k = 1; k < 32; ++k) v[k] = cmul(v[k], TWL[32 * k + lane]);
 #pragma unroll
-        for (int q = 0; q < 8; ++q) {
-            v[8 * j + q] = cmul(v[8 * j + q], t);
-            if (q < 7) t = cmul(t, w);
-        }
+        for (int k = 0; k < 32; ++k) tile[lane * 33 + k] = v[k];
+        __syncwarp();
+#pragma unroll
+        for (int n = 0; n < 32; ++n) v[n] = tile[n * 33 + lane];
+        __syncwarp();
     }
-#pragma unroll
-    for (int k = 0; k < 32; ++k) tile[lane * 33 + k] = v[k];
-    __syncwarp();
-#pragma unroll
-    for (int n = 0; n < 32; ++n) v[n] = tile[n * 33 + lane];
-    __syncwarp();
-    dft32_reg(v);
 }
 
 }  // namespace isar

@@ -164,6 +164,7 @@ struct isar_ctx {
     double* d_H = nullptr;
     int* d_bins = nullptr;
     float2* d_sig_part = nullptr;
+    float2* d_gcol = nullptr;
     unsigned* d_bar = nullptr;     // autofocus grid barrier: [0] counter, [1] timeout flag
     // MTRC / post
     float2* d_st = nullptr;
@@ -315,6 +316,7 @@ int create_impl(isar_ctx* c)
     TRY(dalloc(c, &c->d_H, C));
     TRY(dalloc(c, &c->d_bins, C));
     TRY(dalloc(c, &c->d_sig_part, (size_t)128 * M));
+    TRY(dalloc(c, &c->d_gcol, (size_t)M * C));
     TRY(dalloc(c, &c->d_bar, 4));
     CU(cudaMemsetAsync(c->d_bar, 0, 4 * sizeof(unsigned), c->st));
     TRY(dalloc(c, &c->d_st, (size_t)M * C));
@@ -368,6 +370,7 @@ isar::FEArgs fe_args(isar_ctx* c, float2* cut, int iters)
     a.H = c->d_H;
     a.bins = c->d_bins;
     a.sig_part = c->d_sig_part;
+    a.gcol = c->d_gcol;
     a.bar = c->d_bar;
     a.tw = c->d_tw;
     a.af_cluster = c->af_cluster;

@@ -54,6 +54,7 @@ struct FEArgs {
     double* H;               // [512]
     int* bins;               // [512]
     float2* sig_part;        // [M][128] autofocus partial row sums
+    float2* gcol;            // [512][M] gathered bin columns (cluster engine, M = 1024)
     unsigned* bar;           // [0] grid-barrier counter, [1] barrier timeout flag
     const float2* tw;
     // Autofocus engine: 0 = one cooperative grid (128 CTAs, grid barriers);
