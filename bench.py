@@ -482,9 +482,10 @@ def run_reference(args):
 
 def run_profile(args):
     """Profiling workloads (no timing, no JSON): `plain` images one
-    1024 x 8192 frame warmup + steps times; `batch` runs a batch of 8
-    frames through isar_batch_run (8-CTA cluster autofocus, learned warm
-    start)."""
+    1024 x 8192 frame warmup + steps times; `batch` runs a batch of 8 frames
+    through isar_batch_run with the reference algorithm (8-CTA cluster
+    autofocus, 120 iterations); `learned` the same batch with the learned
+    warm start and the entropy stop criterion."""
     import torch
 
     import isar_imaging_cuda_gb300 as g
@@ -504,17 +505,22 @@ def run_profile(args):
                 ctx.image_device(X[0], V[0], imgs[0], flags)
             ctx.synchronize()
     else:
-        net = g.WSNet(M, stream=s.cuda_stream)
-        net.load_params(g.WARMSTART_WEIGHTS)
+        learned = args.profile == "learned"
+        net = None
+        if learned:
+            net = g.WSNet(M, stream=s.cuda_stream)
+            net.load_params(g.WARMSTART_WEIGHTS)
         with g.Batch(stream=s.cuda_stream, lanes=8) as b:
-            b.set_warmstart(net)
+            if learned:
+                b.set_warmstart(net)
             b.set_tuning(rp, g.Tuning(ra_pair_min=128, ra_rows_per_cta=4, ra_rows_final=4, af_cluster=8,
-                                      af_tol=TOL, af_iters=120, af_cluster_max=0))
+                                      af_tol=TOL if learned else 0.0, af_iters=120, af_cluster_max=0))
             lst = g.Batch.frames((rp, X[i], V[i], flags, imgs[i]) for i in range(nb))
             for _ in range(args.warmup + args.steps):
                 b.run(lst)
             b.synchronize()
-        net.close()
+        if net is not None:
+            net.close()
     torch.cuda.synchronize()
     print("profile workload %s done" % args.profile)
 
@@ -526,7 +532,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu", action="store_true")
-    ap.add_argument("--profile", choices=["plain", "batch"], default=None,
+    ap.add_argument("--profile", choices=["plain", "batch", "learned"], default=None,
                     help="run a profiling workload only (for ncu), no measurement")
     args = ap.parse_args()
     if args.profile:

@@ -859,7 +859,12 @@ k_af_cluster_w1024(AFFrame f, int iters, float tol, const float2* __restrict__ t
         }
     };
 
-    auto cluster_entropy = [&](float s1, float s2, double* slot) {
+    // Entropy of the selected bins, in two halves around a cluster barrier:
+    // this CTA's sums (s1 = sum p, s2 = sum p ln p) into red[32..33], then
+    // after the barrier warp 0 adds the CL CTAs' sums (one remote read per
+    // lane, a fixed-order tree: every CTA gets the same value) and returns
+    // ln S1 - S2 / S1 in lane 0 of warp 0.
+    auto entropy_part = [&](float s1, float s2) {
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) {
             s1 += __shfl_xor_sync(0xffffffffu, s1, o);
@@ -879,16 +884,20 @@ k_af_cluster_w1024(AFFrame f, int iters, float tol, const float2* __restrict__ t
             red[32] = a1;
             red[33] = a2;
         }
-        cl.sync();
-        if (tid == 0) {
-            double S1 = 0.0, S2 = 0.0;
-            for (int q = 0; q < CL; ++q) {
-                const double* rr = cl.map_shared_rank(red, q);
-                S1 += rr[32];
-                S2 += rr[33];
-            }
-            *slot = logf((float)S1) - (float)S2 / (float)S1;
+    };
+    auto entropy_total = [&]() {   // warp 0, after the cluster barrier
+        double S1 = 0.0, S2 = 0.0;
+        if (lane < CL) {
+            const double* rr = cl.map_shared_rank(red, lane);
+            S1 = rr[32];
+            S2 = rr[33];
         }
+#pragma unroll
+        for (int o = 8; o > 0; o >>= 1) {
+            S1 += __shfl_xor_sync(0xffffffffu, S1, o);
+            S2 += __shfl_xor_sync(0xffffffffu, S2, o);
+        }
+        return logf((float)S1) - (float)S2 / (float)S1;
     };
 
     if (f.alt) {
@@ -902,8 +911,13 @@ k_af_cluster_w1024(AFFrame f, int iters, float tol, const float2* __restrict__ t
             }
             float s1 = 0.0f, s2 = 0.0f;
             sweep(false, true, s1, s2);
-            cluster_entropy(s1, s2, &red[41 + k]);
+            entropy_part(s1, s2);
             cl.sync();
+            if (warp == 0) {
+                const float E = entropy_total();
+                if (lane == 0) red[41 + k] = E;
+            }
+            cl.sync();   // red[32..33] are read remotely before the next sweep rewrites them
             e_start[k] = (float)red[41 + k];
         }
         const bool use_alt = e_start[1] < e_start[0];
@@ -921,24 +935,31 @@ k_af_cluster_w1024(AFFrame f, int iters, float tol, const float2* __restrict__ t
 
     float e_prev = 0.0f;   // meaningful in thread 0
     int used = iters;
+    int lg_rows = 0;
+    while ((1 << lg_rows) < rows) ++lg_rows;
+    float2* buf = tiles + AFW::TILE;   // behind P (tile 0 holds P)
 #pragma unroll 1
     for (int it = 0; it < iters; ++it) {
+        // the entropy is needed by the stop criterion or for the last trace
         const bool need_e = tol > 0.0f || it == iters - 1;
         float s1 = 0.0f, s2 = 0.0f;
         sweep(true, need_e, s1, s2);
-        cluster_entropy(s1, s2, &red[44]);
-        if (tid == 0) {
+        if (need_e) entropy_part(s1, s2);
+        cl.sync();   // P and red[32..33] of every CTA are complete
+        if (warp == 0) {
             bool stop = false;
             if (need_e) {
-                const float E = (float)red[44];
+                const float E = entropy_total();
                 stop = tol > 0.0f && it > 0 && fabsf(E - e_prev) <= tol * fabsf(E);
                 e_prev = E;
             }
-            red[40] = stop ? 1.0 : 0.0;
+            if (lane == 0) red[40] = stop ? 1.0 : 0.0;
         }
-        float2* buf = tiles + AFW::TILE;   // behind P (tile 0 holds P)
-        for (int idx = tid; idx < CL * rows; idx += AFW::THREADS) {
-            const int q = idx / rows, ml = idx - q * rows;
+        // this CTA's rows of the cluster sum: slice r of every CTA's P
+#pragma unroll
+        for (int i = 0; i < M / AFW::THREADS; ++i) {
+            const int idx = tid + i * AFW::THREADS;
+            const int q = idx >> lg_rows, ml = idx & (rows - 1);
             buf[idx] = cl.map_shared_rank(P, q)[r * rows + ml];
         }
         __syncthreads();
@@ -952,12 +973,14 @@ k_af_cluster_w1024(AFFrame f, int iters, float tol, const float2* __restrict__ t
                     s.y += v.y;
                 }
                 const float a = sqrtf(s.x * s.x + s.y * s.y);
-                buf[CL * rows + ml] = make_float2(s.x / a, s.y / a);
+                buf[M + ml] = make_float2(s.x / a, s.y / a);
             }
             __syncthreads();
-            for (int idx = tid; idx < CL * rows; idx += AFW::THREADS) {
-                const int q = idx / rows, ml = idx - q * rows;
-                cl.map_shared_rank(ph, q)[r * rows + ml] = buf[CL * rows + ml];
+#pragma unroll
+            for (int i = 0; i < M / AFW::THREADS; ++i) {
+                const int idx = tid + i * AFW::THREADS;
+                const int q = idx >> lg_rows, ml = idx & (rows - 1);
+                cl.map_shared_rank(ph, q)[r * rows + ml] = buf[M + ml];
             }
         }
         cl.sync();
