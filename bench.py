@@ -4,13 +4,15 @@ alignment, centring + cut, fast minimum-entropy autofocus, CZT MTRC).
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
 
-Headline (`value`): the batched + learned pipeline.  A step is one batch of
-B = 32 distinct frames imaged by one CUDA graph (isar_batch_run: per-shape
-lanes, cluster-resident autofocus, learned warm start, entropy stop
-criterion), inputs resident in HBM (2 GiB > L2).  Equal entropy is checked on
-every run: the mean final image entropy of the batch must not exceed the
-plain pipeline's by more than 1e-4 (otherwise the headline falls back to the
-batched reference algorithm, 120 iterations, no warm start, and says so).
+Headline (`value`): the batched pipeline.  A step is one batch of B = 32
+distinct frames imaged by one CUDA graph (isar_batch_run: per-shape lanes,
+cluster-resident autofocus), inputs resident in HBM (2 GiB > L2).  Three
+autofocus arms are tried in order and the first whose images pass the
+equal-entropy check is timed: (1) learned warm start + entropy stop
+criterion, (2) the stop criterion alone (Doppler-tracking start), (3) the
+reference algorithm (120 iterations).  The check: the mean final image
+entropy of the batch must not exceed the plain pipeline's by more than 1e-4.
+Every arm's check is reported.
 `plain` is the single-frame pipeline (isar_image_device, the reference's
 algorithm: cooperative autofocus, 120 iterations), timed the same way.
 `e2e` goes through the public C ABI with pinned host buffers: every step
@@ -36,8 +38,11 @@ sys.path.insert(0, ROOT)
 M, N = 1024, 8192
 C = 512
 B = 32                      # frames per batch step
-TOL = 1e-6                  # autofocus entropy stop criterion of the headline
+TOL = 3e-7                  # autofocus entropy stop criterion (relative change per iteration)
 METRIC = "frames/s @1024×8192 c64: learned+batched vs plain on 1 GB300, equal entropy"
+ARMS = [("learned warm start + entropy stop criterion", True, TOL),
+        ("entropy stop criterion, Doppler-tracking start", False, TOL),
+        ("reference algorithm (120 iterations)", False, 0.0)]
 WORKLOAD = ("full five-stage pipeline, 1024 pulses x 8192 range cells complex64, HPC + MTRC on, "
             "batches of 32 frames")
 # DRAM bytes (read + write) of one range-alignment stage at 1024 x 8192, all
@@ -220,9 +225,9 @@ def run_gb300(args):
     cl = min(cl, probe.tuning().af_cluster_max)
     probe.close()
 
-    def configure(learned):
+    def configure(learned, tol):
         t = g.Tuning(ra_pair_min=128, ra_rows_per_cta=4, ra_rows_final=4, af_cluster=cl,
-                     af_tol=TOL if learned else 0.0, af_iters=120, af_cluster_max=0)
+                     af_tol=tol, af_iters=120, af_cluster_max=0)
         batch.set_warmstart(net if learned else None)
         batch.set_tuning(rp, t)
         tune_ms = batch.autotune(lst)
@@ -231,16 +236,19 @@ def run_gb300(args):
         ent = [image_entropy(imgs[i].cpu().numpy()) for i in range(B)]
         return tune_ms, ent
 
-    tune_ms, e_batch = configure(True)
-    dE = np.array(e_batch) - np.array(e_plain)
-    check = {"tol": TOL, "criterion": "mean(dE) <= 1e-4", "mean_dE": float(dE.mean()), "max_dE": float(dE.max()),
-             "min_dE": float(dE.min()), "frames": B}
-    mode = "batched + learned warm start + entropy stop criterion (tol %g)" % TOL
-    if not dE.mean() <= 1e-4:
-        tune_ms, e_batch = configure(False)
+    # first arm whose images pass the equal-entropy check (the last one is
+    # the reference algorithm itself)
+    check = {"criterion": "mean(dE) <= 1e-4 against the plain pipeline", "frames": B, "arms": []}
+    for name, learned, tol in ARMS:
+        tune_ms, e_batch = configure(learned, tol)
         dE = np.array(e_batch) - np.array(e_plain)
-        check.update(fallback=True, mean_dE_fallback=float(dE.mean()), max_dE_fallback=float(np.abs(dE).max()))
-        mode = "batched reference algorithm (120 iterations, no warm start): learned arm failed the check"
+        ok = bool(dE.mean() <= 1e-4)
+        check["arms"].append({"arm": name, "tol": tol, "mean_dE": float(dE.mean()), "max_dE": float(dE.max()),
+                              "min_dE": float(dE.min()), "frames_worse_1e-4": int((dE > 1e-4).sum()),
+                              "passed": ok})
+        if ok or tol == 0.0:
+            break
+    mode = "batched, " + name
     lanes = batch.lanes()
     tuning = batch.tuning(rp).as_dict()
 

@@ -95,7 +95,8 @@ typedef struct {
     int af_cluster;           /* autofocus engine: 0 = one cooperative grid of 128    */
                               /* CTAs; 4, 8, 16 = one thread-block cluster per frame  */
     float af_tol;             /* stop once the entropy of the selected bins changes   */
-                              /* by <= af_tol * |entropy| (cluster engine; 0 = off)   */
+                              /* by <= af_tol * |entropy| per iteration (mean over 4, */
+                              /* checked every 4th iteration; cluster engine; 0 = off)*/
     int af_iters;             /* autofocus iterations, or the cap with af_tol (120)   */
     int af_cluster_max;       /* out: largest af_cluster this device can launch       */
 } isar_tuning;

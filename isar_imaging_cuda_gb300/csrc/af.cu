@@ -13,6 +13,19 @@ namespace isar {
 
 constexpr int C = kRangeCut;
 
+// The cluster engines' entropy of the selected bins (stop criterion, choice
+// of start, trace) sums p log2 p with the hardware base-2 logarithm
+// (__log2f, ~2^-22 relative error, a few instructions instead of ~20 for
+// logf) and converts once: H = ln S1 - ln 2 * S2 / S1.
+constexpr float kLn2 = 0.693147180559945309f;
+
+// The stop criterion compares the entropy every kStopEvery iterations: stop
+// at iteration it (a multiple of kStopEvery, it > 0, before its update) once
+// |E(it) - E(it - kStopEvery)| <= kStopEvery * tol * |E(it)|, i.e. once the
+// entropy changes by at most tol * |E| per iteration on average.  Iterations
+// in between skip the entropy terms and its cluster reduction.
+constexpr int kStopEvery = 4;
+
 // Column max of |cut| over rows [0, min(M,256)) per CTA of R rows, and the
 // Doppler sums s[m] = sum_c conj(x[m,c]) x[m+1,c] (one warp per row).
 __global__ void __launch_bounds__(256)
@@ -445,7 +458,7 @@ k_af_persist(const float2* __restrict__ cut, const int* __restrict__ bins, const
 // reduces rows [r*M/CL, (r+1)*M/CL) over the CL partials (distributed shared
 // memory, fixed rank order), normalises and stores the new phase into every
 // CTA's copy; cluster barrier.  The entropy of the selected bins,
-// E = ln S1 - S2/S1 with S1 = sum |T|^2, S2 = sum |T|^2 ln |T|^2, comes out of
+// E = ln S1 - ln 2 * S2/S1 with S1 = sum |T|^2, S2 = sum |T|^2 log2 |T|^2, comes out of
 // the same epilogue and drives the optional stop criterion.
 // Only hardware cluster barriers: no spin-waits.
 // ---------------------------------------------------------------------------
@@ -544,7 +557,7 @@ k_af_cluster(AFFrame f, int iters, float tol, const float2* __restrict__ tw)
                                    const float p = v.x * v.x + v.y * v.y;
                                    if (ent) {
                                        s1 += p;
-                                       if (p > 0.0f) s2 += p * logf(p);
+                                       if (p > 0.0f) s2 += p * __log2f(p);
                                    }
                                    sm[fpad(i)] = cscale(v, sqrtf(p));
                                },
@@ -614,7 +627,7 @@ k_af_cluster(AFFrame f, int iters, float tol, const float2* __restrict__ tw)
                     S1 += rr[32];
                     S2 += rr[33];
                 }
-                red[41 + k] = logf((float)S1) - (float)S2 / (float)S1;
+                red[41 + k] = logf((float)S1) - kLn2 * (float)S2 / (float)S1;
             }
             cl.sync();
             e_start[k] = (float)red[41 + k];
@@ -632,13 +645,14 @@ k_af_cluster(AFFrame f, int iters, float tol, const float2* __restrict__ tw)
         __syncthreads();
     }
 
-    float e_prev = 0.0f;   // meaningful in thread 0
+    float e_prev = 0.0f, e_last = 0.0f;   // meaningful in thread 0
     int used = iters;
 #pragma unroll 1
     for (int it = 0; it < iters; ++it) {
         // the entropy is needed by the stop criterion, and for the trace at
         // the last iteration; elsewhere its logarithms are skipped
-        const bool need_e = tol > 0.0f || it == iters - 1;
+        const bool check = tol > 0.0f && it % kStopEvery == 0;
+        const bool need_e = check || it == iters - 1;
         float s1 = 0.0f, s2 = 0.0f;
         sweep(true, need_e, s1, s2);
         // Entropy sums: float per warp, double per CTA (red[32..33]) and per
@@ -672,9 +686,12 @@ k_af_cluster(AFFrame f, int iters, float tol, const float2* __restrict__ tw)
             }
             bool stop = false;
             if (need_e) {
-                const float E = logf((float)S1) - (float)S2 / (float)S1;
-                stop = tol > 0.0f && it > 0 && fabsf(E - e_prev) <= tol * fabsf(E);
-                e_prev = E;
+                const float E = logf((float)S1) - kLn2 * (float)S2 / (float)S1;
+                if (check) {
+                    stop = it > 0 && fabsf(E - e_prev) <= (float)kStopEvery * tol * fabsf(E);
+                    e_prev = E;
+                }
+                e_last = E;
             }
             red[40] = stop ? 1.0 : 0.0;
         }
@@ -713,7 +730,7 @@ k_af_cluster(AFFrame f, int iters, float tol, const float2* __restrict__ tw)
     for (int m = r * rows + tid; m < (r + 1) * rows; m += A::THREADS) f.phase[m] = ph[m];
     if (r == 0 && tid == 0 && f.stat) {
         f.stat[0] = used;
-        f.stat[1] = __float_as_int(e_prev);
+        f.stat[1] = __float_as_int(e_last);
     }
 }
 
@@ -823,7 +840,7 @@ k_af_cluster_w1024(AFFrame f, int iters, float tol, const float2* __restrict__ t
                         const float p = v[k].x * v[k].x + v[k].y * v[k].y;
                         if (ent) {
                             s1 += p;
-                            if (p > 0.0f) s2 += p * logf(p);
+                            if (p > 0.0f) s2 += p * __log2f(p);
                         }
                         const float a = p > 0.0f ? p * rsqrtf(p) : 0.0f;
                         v[k] = make_float2(v[k].x * a, -v[k].y * a);   // conj(T |T|)
@@ -860,10 +877,10 @@ k_af_cluster_w1024(AFFrame f, int iters, float tol, const float2* __restrict__ t
     };
 
     // Entropy of the selected bins, in two halves around a cluster barrier:
-    // this CTA's sums (s1 = sum p, s2 = sum p ln p) into red[32..33], then
+    // this CTA's sums (s1 = sum p, s2 = sum p log2 p) into red[32..33], then
     // after the barrier warp 0 adds the CL CTAs' sums (one remote read per
     // lane, a fixed-order tree: every CTA gets the same value) and returns
-    // ln S1 - S2 / S1 in lane 0 of warp 0.
+    // ln S1 - ln 2 * S2 / S1 in lane 0 of warp 0.
     auto entropy_part = [&](float s1, float s2) {
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) {
@@ -897,7 +914,7 @@ k_af_cluster_w1024(AFFrame f, int iters, float tol, const float2* __restrict__ t
             S1 += __shfl_xor_sync(0xffffffffu, S1, o);
             S2 += __shfl_xor_sync(0xffffffffu, S2, o);
         }
-        return logf((float)S1) - (float)S2 / (float)S1;
+        return logf((float)S1) - kLn2 * (float)S2 / (float)S1;
     };
 
     if (f.alt) {
@@ -933,7 +950,7 @@ k_af_cluster_w1024(AFFrame f, int iters, float tol, const float2* __restrict__ t
         __syncthreads();
     }
 
-    float e_prev = 0.0f;   // meaningful in thread 0
+    float e_prev = 0.0f, e_last = 0.0f;   // meaningful in thread 0
     int used = iters;
     int lg_rows = 0;
     while ((1 << lg_rows) < rows) ++lg_rows;
@@ -941,7 +958,8 @@ k_af_cluster_w1024(AFFrame f, int iters, float tol, const float2* __restrict__ t
 #pragma unroll 1
     for (int it = 0; it < iters; ++it) {
         // the entropy is needed by the stop criterion or for the last trace
-        const bool need_e = tol > 0.0f || it == iters - 1;
+        const bool check = tol > 0.0f && it % kStopEvery == 0;
+        const bool need_e = check || it == iters - 1;
         float s1 = 0.0f, s2 = 0.0f;
         sweep(true, need_e, s1, s2);
         if (need_e) entropy_part(s1, s2);
@@ -950,8 +968,11 @@ k_af_cluster_w1024(AFFrame f, int iters, float tol, const float2* __restrict__ t
             bool stop = false;
             if (need_e) {
                 const float E = entropy_total();
-                stop = tol > 0.0f && it > 0 && fabsf(E - e_prev) <= tol * fabsf(E);
-                e_prev = E;
+                if (check) {
+                    stop = it > 0 && fabsf(E - e_prev) <= (float)kStopEvery * tol * fabsf(E);
+                    e_prev = E;
+                }
+                e_last = E;
             }
             if (lane == 0) red[40] = stop ? 1.0 : 0.0;
         }
@@ -992,7 +1013,7 @@ k_af_cluster_w1024(AFFrame f, int iters, float tol, const float2* __restrict__ t
     for (int m = r * rows + tid; m < (r + 1) * rows; m += AFW::THREADS) f.phase[m] = ph[m];
     if (r == 0 && tid == 0 && f.stat) {
         f.stat[0] = used;
-        f.stat[1] = __float_as_int(e_prev);
+        f.stat[1] = __float_as_int(e_last);
     }
 }
 

@@ -136,8 +136,14 @@ struct TwTwoLevel<TwShared<N, F, T>> {
     static constexpr bool value = TwShared<N, F, T>::kTwoLevel;
 };
 
-template <int N, int R, int NS, bool INV, bool FIRST, bool LAST, class Src, class Dst, class Tw>
-__device__ __forceinline__ void fft_pass(Src& src, Dst& dst, float2* sm, int lt, const Tw& tw, bool active)
+// No-op hook of team_fft.
+struct NoHook {
+    __device__ __forceinline__ void operator()() const {}
+};
+
+template <int N, int R, int NS, bool INV, bool FIRST, bool LAST, class Src, class Dst, class Tw, class Hook>
+__device__ __forceinline__ void fft_pass(Src& src, Dst& dst, float2* sm, int lt, const Tw& tw, bool active,
+                                         Hook& hook)
 {
     constexpr int T = N / 16;
     constexpr int B = 16 / R;
@@ -160,6 +166,7 @@ __device__ __forceinline__ void fft_pass(Src& src, Dst& dst, float2* sm, int lt,
     // Both barriers of a pass are executed by every thread: teams narrower than
     // a warp share warps, so a barrier inside `if (active)` would diverge.
     __syncthreads();
+    if constexpr (FIRST) hook();   // every src() read of the CTA is done
     if (active) {
 #pragma unroll
         for (int b = 0; b < B; ++b) {
@@ -210,13 +217,14 @@ __device__ __forceinline__ void fft_pass(Src& src, Dst& dst, float2* sm, int lt,
     __syncthreads();
 }
 
-template <int N, bool INV, int PASS, int NS, class Src, class Dst, class Tw>
-__device__ __forceinline__ void fft_passes(Src& src, Dst& dst, float2* sm, int lt, const Tw& tw, bool active)
+template <int N, bool INV, int PASS, int NS, class Src, class Dst, class Tw, class Hook>
+__device__ __forceinline__ void fft_passes(Src& src, Dst& dst, float2* sm, int lt, const Tw& tw, bool active,
+                                           Hook& hook)
 {
     using S = FFTShape<N>;
     constexpr int R = (PASS < S::NP16) ? 16 : (1 << S::REM);
-    fft_pass<N, R, NS, INV, PASS == 0, PASS == S::NPASS - 1>(src, dst, sm, lt, tw, active);
-    if constexpr (PASS + 1 < S::NPASS) fft_passes<N, INV, PASS + 1, NS * R>(src, dst, sm, lt, tw, active);
+    fft_pass<N, R, NS, INV, PASS == 0, PASS == S::NPASS - 1>(src, dst, sm, lt, tw, active, hook);
+    if constexpr (PASS + 1 < S::NPASS) fft_passes<N, INV, PASS + 1, NS * R>(src, dst, sm, lt, tw, active, hook);
 }
 
 // One team transform.  src(i) -> float2 for i in [0,N) (first pass, may read
@@ -226,11 +234,14 @@ __device__ __forceinline__ void fft_passes(Src& src, Dst& dst, float2* sm, int l
 // A team with active == false does no work but keeps the barriers.
 // Contains __syncthreads(): every thread of the CTA must call it.
 // tw: the global kTwN table (TwGlobal) or a TwShared<N> accessor.
-template <int N, bool INV, class Src, class Dst, class Tw>
-__device__ __forceinline__ void team_fft(Src src, Dst dst, float2* sm, int lt, const Tw& tw, bool active = true)
+// hook() runs in every thread once all src() reads of the CTA are done
+// (after the first pass's load barrier), e.g. to refill the source buffer.
+template <int N, bool INV, class Src, class Dst, class Tw, class Hook = NoHook>
+__device__ __forceinline__ void team_fft(Src src, Dst dst, float2* sm, int lt, const Tw& tw, bool active = true,
+                                         Hook hook = Hook{})
 {
     static_assert(N >= 32 && (N & (N - 1)) == 0 && N <= kTwN, "FFT size");
-    fft_passes<N, INV, 0, 1>(src, dst, sm, lt, tw, active);
+    fft_passes<N, INV, 0, 1>(src, dst, sm, lt, tw, active, hook);
 }
 
 template <int N, bool INV, class Src, class Dst>
@@ -239,6 +250,137 @@ __device__ __forceinline__ void team_fft(Src src, Dst dst, float2* sm, int lt, c
 {
     team_fft<N, INV>(src, dst, sm, lt, TwGlobal{tw}, active);
 }
+
+// ---------------------------------------------------------------------------
+// Row transforms of the range alignment.  At N = 8192 a CTA of 512 threads
+// runs the transform as 16 x 512: one radix-16 pass over the whole CTA
+// (thread t takes x[t + 512 r], r < 16, and multiplies by W_8192^(t k0)),
+// one exchange through shared memory, then sixteen independent 512-point
+// transforms, one per warp (warp k0 takes row k0): a 16-point DFT in
+// registers over m1 (t = m0 + 32 m1, m0 = lane), the twiddles W_512^(m0 k1),
+// a transpose through the warp's own part of the scratch (__syncwarp only),
+// a 16-point DFT over b (m0 = 2 b + a) and a radix-2 step between lanes
+// l and l ^ 16 (shuffles).  Two block barriers per transform instead of the
+// eight of the four-pass Stockham transform.
+// Output X[k0 + 16 k1 + 256 q + 4096 a] lands in register slot q of lane
+// k1 + 16 a of warp k0.
+// ---------------------------------------------------------------------------
+
+// Twiddles of row_fft<N>: the two-level table of TwShared<N>, followed at
+// N = 8192 by the step twiddles W_512^(m k) of the warp transforms at
+// [32 k + m] (k < 16, m < 32).
+template <int N>
+struct RowTw {
+    using Two = TwShared<N>;
+    static constexpr int kStep = N == 8192 ? 512 : 0;
+    static constexpr int kEntries = Two::kEntries + kStep;
+    const float2* p;
+    __device__ __forceinline__ float2 operator()(int e, int n) const { return Two{p}(e, n); }
+    __device__ __forceinline__ float2 step(int k, int m) const { return p[Two::kEntries + 32 * k + m]; }
+    __device__ __forceinline__ static void fill(float2* t, const float2* __restrict__ g, int tid, int nthreads)
+    {
+        Two::fill(t, g, tid, nthreads);
+        if constexpr (kStep > 0)
+            for (int i = tid; i < kStep; i += nthreads)
+                t[Two::kEntries + i] = g[(((i >> 5) * (i & 31) * 16) & (N - 1)) * (kTwN / N)];
+    }
+};
+template <int N>
+struct TwTwoLevel<RowTw<N>> {
+    static constexpr bool value = TwShared<N>::kTwoLevel;
+};
+
+// 8192-point transform, one CTA of 512 threads (see above).  sm: 16 x 544
+// float2 (FFTShape<8192>::SMEM).  src(i) is called for i = lt + 512 r in
+// order r = 0..15 and must not read sm; dst(i, v, slot) must not write sm.
+// Contains __syncthreads(): every thread of the CTA must call it.
+template <bool INV, class Src, class Dst, class Hook>
+__device__ __forceinline__ void fft8192(Src& src, Dst& dst, float2* sm, int lt, const RowTw<8192>& tw, Hook& hook)
+{
+    constexpr int N = 8192;
+    constexpr int RS = 544;   // scratch row stride (float2)
+    const int lane = lt & 31, w = lt >> 5;
+    float2 v[16];
+#pragma unroll
+    for (int r = 0; r < 16; ++r) v[r] = src(lt + 512 * r);
+    __syncthreads();   // the previous transform's warps are done with the scratch
+    hook();
+    dft_reg<16, INV>(v);
+    {
+        // W_8192^(lt k0): look up k0 = 1, 2, 4, 8, form the others as products
+        float2 t[16];
+        t[1] = tw(lt, N);
+        t[2] = tw(2 * lt, N);
+        t[4] = tw(4 * lt, N);
+        t[8] = tw(8 * lt, N);
+        t[3] = cmul(t[2], t[1]);
+        t[5] = cmul(t[4], t[1]);
+        t[6] = cmul(t[4], t[2]);
+        t[7] = cmul(t[4], t[3]);
+#pragma unroll
+        for (int k = 9; k < 16; ++k) t[k] = cmul(t[8], t[k - 8]);
+#pragma unroll
+        for (int k = 1; k < 16; ++k) {
+            float2 x = t[k];
+            if (INV) x.y = -x.y;
+            v[k] = cmul(v[k], x);
+        }
+    }
+#pragma unroll
+    for (int k = 0; k < 16; ++k) sm[k * RS + lt] = v[k];
+    __syncthreads();
+    float2* row = sm + w * RS;
+#pragma unroll
+    for (int m1 = 0; m1 < 16; ++m1) v[m1] = row[lane + 32 * m1];
+    dft_reg<16, INV>(v);
+#pragma unroll
+    for (int k = 1; k < 16; ++k) {
+        float2 x = tw.step(k, lane);
+        if (INV) x.y = -x.y;
+        v[k] = cmul(v[k], x);
+    }
+    __syncwarp();   // the row is read: the tile may overwrite it
+#pragma unroll
+    for (int k = 0; k < 16; ++k) row[lane * 17 + k] = v[k];
+    __syncwarp();
+    const int k1 = lane & 15, a = lane >> 4;
+#pragma unroll
+    for (int b = 0; b < 16; ++b) v[b] = row[(2 * b + a) * 17 + k1];
+    dft_reg<16, INV>(v);
+    const float c[16] = {1.000000000f,  0.980785280f,  0.923879533f,  0.831469612f, 0.707106781f,  0.555570233f,
+                         0.382683432f,  0.195090322f,  0.000000000f,  -0.195090322f, -0.382683432f, -0.555570233f,
+                         -0.707106781f, -0.831469612f, -0.923879533f, -0.980785280f};
+    const float s[16] = {0.000000000f, 0.195090322f, 0.382683432f, 0.555570233f, 0.707106781f, 0.831469612f,
+                         0.923879533f, 0.980785280f, 1.000000000f, 0.980785280f, 0.923879533f, 0.831469612f,
+                         0.707106781f, 0.555570233f, 0.382683432f, 0.195090322f};
+#pragma unroll
+    for (int q = 0; q < 16; ++q) {
+        float2 o;
+        o.x = __shfl_xor_sync(0xffffffffu, v[q].x, 16);
+        o.y = __shfl_xor_sync(0xffffffffu, v[q].y, 16);
+        const float2 d0 = a ? o : v[q], d1 = a ? v[q] : o;
+        const float sn = INV ? s[q] : -s[q];   // W_32^q (forward), conj for the inverse
+        const float2 t = make_float2(d1.x * c[q] - d1.y * sn, d1.x * sn + d1.y * c[q]);
+        const float2 y = a ? csub(d0, t) : cadd(d0, t);
+        dst(w + 16 * k1 + 256 * q + 4096 * a, y, q);
+    }
+}
+
+// Row transform used by the range alignment: with WARP, fft8192 at
+// N = 8192; otherwise the Stockham team transform (same src / dst / hook
+// contract).  fft8192 hands the outputs of a warp to dst with a stride of 16
+// elements across lanes, so kernels that store the transformed rows keep the
+// team transform (its outputs are lane-contiguous, stores coalesce).
+template <int N, bool INV, bool WARP, class Src, class Dst, class Hook>
+__device__ __forceinline__ void row_fft(Src src, Dst dst, float2* sm, int lt, const RowTw<N>& tw, Hook hook)
+{
+    if constexpr (WARP && N == 8192) fft8192<INV>(src, dst, sm, lt, tw, hook);
+    else team_fft<N, INV>(src, dst, sm, lt, tw, true, hook);
+}
+
+// Output index of register slot `slot` of thread lt for row_fft<N, *, WARP>.
+template <int N, bool WARP>
+__device__ __forceinline__ int row_out_index(int lt, int slot);
 
 // Output index of register slot `slot` for thread lt (the LAST pass mapping),
 // so that callers can revisit their outputs after the transform.
@@ -249,6 +391,17 @@ __device__ __forceinline__ int fft_out_index(int lt, int slot)
     constexpr int R = (S::NPASS - 1 < S::NP16) ? 16 : (1 << S::REM);
     const int b = slot / R, r = slot % R;
     return lt + b * S::T + r * (N / R);
+}
+
+template <int N, bool WARP>
+__device__ __forceinline__ int row_out_index(int lt, int slot)
+{
+    if constexpr (WARP && N == 8192) {
+        const int lane = lt & 31;
+        return (lt >> 5) + 16 * (lane & 15) + 256 * slot + 4096 * (lane >> 4);
+    } else {
+        return fft_out_index<N>(lt, slot);
+    }
 }
 
 // ---------------------------------------------------------------------------

@@ -165,7 +165,8 @@ struct isar_ctx {
     int* d_bins = nullptr;
     float2* d_sig_part = nullptr;
     float2* d_gcol = nullptr;
-    unsigned* d_bar = nullptr;     // autofocus grid barrier: [0] counter, [1] timeout flag
+    unsigned* d_bar = nullptr;     // [0] autofocus grid-barrier counter, [1] its timeout flag,
+                                   // [2] range-alignment row-copy timeout flag
     // MTRC / post
     float2* d_st = nullptr;
     float2* d_st2 = nullptr;
@@ -353,6 +354,7 @@ isar::RAArgs ra_args(isar_ctx* c, const float2* x, float2* y, bool hpc, bool hrr
     a.rpc = c->ra_rpc;
     a.rpc_final = c->ra_rpc_final;
     a.given_shifts = c->ra_given ? 1 : 0;
+    a.err = c->d_bar + 2;
     return a;
 }
 
@@ -406,6 +408,9 @@ isar::PostArgs post_args(isar_ctx* c, float2* cut, int flags, float* img)
 
 int run_range_align(isar_ctx* c, const float2* x, float2* y, const double* d_vel, int flags)
 {
+    // rows are staged into shared memory by bulk copies (16-byte granules)
+    if ((reinterpret_cast<uintptr_t>(x) | reinterpret_cast<uintptr_t>(y)) & 15)
+        return fail(ISAR_EINVAL, "echo and range-profile buffers must be 16-byte aligned");
     const bool hpc = (flags & ISAR_FLAG_HPC) && c->r.data_type == ISAR_DATA_STRETCH;
     if (hpc) {
         if (!d_vel) return fail(ISAR_EINVAL, "ISAR_FLAG_HPC needs the pulse velocities");
@@ -489,15 +494,18 @@ int check_ctx(isar_ctx* c)
 }
 
 // Waits for the context stream and reports device-side failures: the
-// autofocus kernel's grid barrier sets a flag instead of waiting forever.
+// autofocus kernel's grid barrier and the range-alignment row copies set a
+// flag instead of waiting forever.
 int sync_status(isar_ctx* c)
 {
     CU(cudaStreamSynchronize(c->st));
-    unsigned flag = 0;
-    CU(cudaMemcpy(&flag, c->d_bar + 1, sizeof(unsigned), cudaMemcpyDeviceToHost));
-    if (flag) {
-        CU(cudaMemsetAsync(c->d_bar, 0, 2 * sizeof(unsigned), c->st));
-        return fail(ISAR_ECUDA, "autofocus grid barrier timed out (image of this frame is invalid)");
+    unsigned flag[3] = {0, 0, 0};
+    CU(cudaMemcpy(flag, c->d_bar, sizeof(flag), cudaMemcpyDeviceToHost));
+    if (flag[1] || flag[2]) {
+        CU(cudaMemsetAsync(c->d_bar, 0, 3 * sizeof(unsigned), c->st));
+        CU(cudaStreamSynchronize(c->st));
+        return fail(ISAR_ECUDA, flag[1] ? "autofocus grid barrier timed out (image of this frame is invalid)"
+                                        : "range-alignment row copy timed out (image of this frame is invalid)");
     }
     return ISAR_OK;
 }

@@ -167,6 +167,8 @@ int check_frames(const isar_batch_frame* f, int n)
     if (!f || n <= 0) return fail(ISAR_EINVAL, "empty batch");
     for (int i = 0; i < n; ++i)
         if (!f[i].d_echo || !f[i].d_img) return fail(ISAR_EINVAL, "frame %d: null echo or image", i);
+        else if (reinterpret_cast<uintptr_t>(f[i].d_echo) & 15)
+            return fail(ISAR_EINVAL, "frame %d: echo buffer must be 16-byte aligned", i);
     return ISAR_OK;
 }
 

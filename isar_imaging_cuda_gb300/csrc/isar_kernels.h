@@ -40,6 +40,7 @@ struct RAArgs {
     int rpc;                 // rows per CTA for the accumulate kernel
     int rpc_final;           // rows per CTA for the final transform
     int given_shifts;        // use the shifts already in `shifts` (test hook)
+    unsigned* err;           // set when a row-copy wait runs out (rows invalid)
 };
 
 struct FEArgs {
@@ -62,8 +63,9 @@ struct FEArgs {
     // (distributed shared memory, no grid barrier).
     int af_cluster;
     // Entropy stop criterion (cluster engine): stop once the entropy of the
-    // selected bins changes by <= tol * |entropy| between two iterations;
-    // 0 runs all `iters` (the reference's fixed count).
+    // selected bins changes by <= tol * |entropy| per iteration (mean over
+    // the 4 iterations between two checks); 0 runs all `iters` (the
+    // reference's fixed count).
     float tol;
     int* af_stat;            // [0] iterations applied, [1] entropy (float bits), [2] warm start used,
                              // [3], [4] start entropies (float bits); may be null

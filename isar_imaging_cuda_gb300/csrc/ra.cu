@@ -69,13 +69,96 @@ struct RowPhase {
     }
 };
 
+// Linear row phase exp(-j 2 pi sq n / 2^64) of the same 16 elements: exact
+// at r = 0 and r = 8, one rotor step cis(-sq D) in between.
+template <int N>
+struct LinPhase {
+    float2 C, R;
+    uint64_t p0, d;
+    __device__ __forceinline__ void init(int64_t sq, int lt)
+    {
+        constexpr uint64_t D = N / 16;
+        p0 = 0ull - (uint64_t)sq * (uint64_t)lt;
+        d = 0ull - (uint64_t)sq * D;
+        R = cis_frac64(d);
+    }
+    __device__ __forceinline__ float2 at(int r)
+    {
+        if (r == 0 || r == 8) C = cis_frac64(p0 + (uint64_t)r * d);
+        else C = cmul(C, R);
+        return C;
+    }
+};
+
+// One-row staging buffer in shared memory, filled by bulk asynchronous copies
+// (cp.async.bulk, completion counted on an mbarrier).  The row kernels issue
+// the copy of their next row as soon as every thread has read the current
+// one (team_fft's hook), so the HBM read of row r+1 overlaps the transform
+// of row r.  Waits are bounded: a wait that runs out sets *err and the CTA
+// carries on (its rows are then invalid and the host reports the failure).
+constexpr unsigned kRowWaitLimit = 1u << 22;
+
+struct RowStage {
+    float2* buf;      // N float2, 16-byte aligned
+    uint64_t* bar;    // mbarrier
+    unsigned* err;    // timeout flag (global)
+    uint32_t parity;
+
+    __device__ __forceinline__ static uint32_t saddr(const void* p)
+    {
+        return (uint32_t)__cvta_generic_to_shared(p);
+    }
+    // thread 0, before the CTA's first barrier
+    __device__ __forceinline__ void init() const
+    {
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(saddr(bar)) : "memory");
+        asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+    }
+    // thread 0: copy `bytes` from global src into buf
+    __device__ __forceinline__ void issue(const void* src, uint32_t bytes) const
+    {
+        asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+        asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(saddr(bar)), "r"(bytes)
+                     : "memory");
+        asm volatile(
+            "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];\n" ::"r"(
+                saddr(buf)),
+            "l"(src), "r"(bytes), "r"(saddr(bar))
+            : "memory");
+    }
+    __device__ __forceinline__ bool try_wait_once() const
+    {
+        uint32_t done;
+        asm volatile(
+            "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+            : "=r"(done)
+            : "r"(saddr(bar)), "r"(parity)
+            : "memory");
+        return done != 0;
+    }
+    // every thread: wait for the copy in flight
+    __device__ __forceinline__ void wait()
+    {
+        bool ok = false;
+        for (unsigned i = 0; i < kRowWaitLimit && !ok; ++i) {
+            ok = try_wait_once();
+            if (!ok && i > 64) __nanosleep(64);
+        }
+        if (!ok) {
+            atomicOr(err, 1u);
+            for (unsigned i = 0; i < kRowWaitLimit && !try_wait_once(); ++i) __nanosleep(256);
+        }
+        parity ^= 1u;
+    }
+};
+
 // Twiddle table of the range-alignment kernels: the two-level shared table
 // above 2048 points (1.5 KB at N = 8192, filled by every CTA).  Measured
 // alternatives were slower: a full N-entry table (read with 32-word strides
 // by the radix-16 passes: many-way bank conflicts) and one exact table per
 // pass (69 KB per CTA: the fill costs more than the saved multiplies).
 template <int N>
-using RaTw = TwShared<N>;
+using RaTw = RowTw<N>;
 
 // HPC coefficient per pulse: alpha_m = coef * v_m / Fs^2 in cycles per n^2,
 // coef = -4*pi*(B/Tp)/c (high_speed_compensation.cu:17-18).
@@ -297,41 +380,58 @@ __device__ __forceinline__ void two_sum_acc(float& s, float& c, float x)
     s = t;
 }
 
-// One row: IFFT(x * win * exp(j 2 pi (alpha n^2 - S n / N))) / N, |.|^2
-// accumulated (compensated) into acc/accl (register slots of this thread).
-template <int N, class Tw>
-__device__ __forceinline__ void ra_row_power(const float2* __restrict__ xr, const float* __restrict__ win,
-                                             int64_t h, int64_t sq, float* acc, float* accl, float2* sm, int lt,
-                                             const Tw& tw)
+// The rows enter every transform pre-multiplied: level 0 reads the spectra
+// x and stores u = x * win * exp(j 2 pi alpha n^2) / N (the window, the
+// high-speed-compensation chirp and the IFFT's 1/N, which is exact) into the
+// row buffer xw; later levels and the final transform read u and apply only
+// the alignment ramp exp(-j 2 pi S n / N).  IFFT(u * ramp) is then the range
+// profile itself, with no per-element window, chirp or scaling work.
+
+// One row: IFFT(u * ramp), |.|^2 accumulated (compensated) into acc/accl
+// (register slots of this thread).  sr: the row in the staging buffer.
+// Level 0 (raw): sr holds x, u is formed and stored to ur (global);
+// otherwise sr holds u.  hook: see team_fft.  WARP: see row_fft.
+template <int N, bool RAW, bool WARP, class Tw, class Hook>
+__device__ __forceinline__ void ra_row_power(const float2* sr, float2* ur, const float* __restrict__ win, int64_t h,
+                                             int64_t sq, float* acc, float* accl, float2* sm, int lt, const Tw& tw,
+                                             Hook hook)
 {
-    const float invN = 1.0f / (float)N;
-    RowPhase<N> rp;
-    rp.init(h, sq, lt);
-    team_fft<N, true>(
-        [&](int i) {   // i = lt + r N/16, r = 0..15 in order
-            const float2 v = xr[i];
-            return cscale(cmul(v, rp.at((i - lt) / (N / 16))), __ldg(&win[i]));
-        },
-        [&](int, float2 v, int slot) {
-            const float re = v.x * invN, im = v.y * invN;
-            two_sum_acc(acc[slot], accl[slot], re * re + im * im);
-        },
-        sm, lt, tw);
+    auto sink = [&](int, float2 v, int slot) { two_sum_acc(acc[slot], accl[slot], v.x * v.x + v.y * v.y); };
+    if constexpr (RAW) {
+        const float invN = 1.0f / (float)N;
+        RowPhase<N> rp;
+        rp.init(h, sq, lt);
+        row_fft<N, true, WARP>(
+            [&](int i) {   // i = lt + r N/16, r = 0..15 in order
+                const float2 u = cscale(cmul(sr[i], rp.at((i - lt) / (N / 16))), __ldg(&win[i]) * invN);
+                ur[i] = u;   // sq = 0 at level 0: the phase is the chirp alone
+                return u;
+            },
+            sink, sm, lt, tw, hook);
+    } else {
+        LinPhase<N> lp;
+        lp.init(sq, lt);
+        row_fft<N, true, WARP>([&](int i) { return cmul(sr[i], lp.at((i - lt) / (N / 16))); }, sink, sm, lt, tw,
+                               hook);
+    }
 }
 
 // Level kernel, one CTA per pair j of groups (G_2j, G_2j+1) of size s=2^level.
-// Level 0 transforms both rows; level >= 1 transforms the second halves R_k
-// of both groups and adds the carried envelopes left_prev[k] of the first
-// halves.  Writes the pair shift, adds it to S of the rows of G_2j+1 and
-// stores env^2(G_2j) as left_next[j].
-template <int N>
+// Level 0 (RAW) transforms both rows from x and stores their pre-multiplied
+// rows into xw; level >= 1 transforms the second halves R_k of both groups
+// from xw and adds the carried envelopes left_prev[k] of the first halves.
+// Writes the pair shift, adds it to S of the rows of G_2j+1 and stores
+// env^2(G_2j) as left_next[j].
+template <int N, bool RAW>
 __global__ void __launch_bounds__(N / 16)
-k_ra_pair(const float2* __restrict__ x, const float* __restrict__ win, const int64_t* __restrict__ hq,
+k_ra_pair(const float2* __restrict__ x, float2* xw, const float* __restrict__ win, const int64_t* __restrict__ hq,
           double* __restrict__ S, int64_t* __restrict__ SQ, int level, const float* __restrict__ left_prev,
-          int lstride, float* __restrict__ left_next, float* shift_out, int given, const float2* __restrict__ tw)
+          int lstride, float* __restrict__ left_next, float* shift_out, int given, const float2* __restrict__ tw,
+          unsigned* err)
 {
     using F = FFTShape<N>;
     extern __shared__ float4 dyn_smem[];
+    __shared__ __align__(8) uint64_t bar;
     float* sm_f = reinterpret_cast<float*>(dyn_smem);
     float* ea = sm_f + 2 * F::SMEM;
     float* eb = ea + N;
@@ -340,27 +440,42 @@ k_ra_pair(const float2* __restrict__ x, const float* __restrict__ win, const int
     const int j = blockIdx.x;
     float2* sm = reinterpret_cast<float2*>(sm_f);
     float2* twt = reinterpret_cast<float2*>(eb + N);
+    // rows of this CTA in order: R_2j then R_2j+1 (one row each at level 0)
+    const int nr = (level == 0) ? 1 : s / 2;
+    auto row_of = [&](int t) {
+        const int k = 2 * j + t / nr;
+        return ((level == 0) ? k : k * s + s / 2) + t % nr;
+    };
+    const float2* src = RAW ? x : xw;
+    RowStage st{twt + RaTw<N>::kEntries, &bar, err, 0u};
+    if (lt == 0) {
+        st.init();
+        st.issue(src + (size_t)row_of(0) * N, N * sizeof(float2));
+    }
     RaTw<N>::fill(twt, tw, lt, F::T);
     __syncthreads();
     const RaTw<N> tws{twt};
 #pragma unroll 1
     for (int g = 0; g < 2; ++g) {
         const int k = 2 * j + g;
-        const int r0 = (level == 0) ? k : k * s + s / 2;
-        const int nr = (level == 0) ? 1 : s / 2;
         float acc[16], accl[16];
 #pragma unroll
         for (int q = 0; q < 16; ++q) acc[q] = accl[q] = 0.0f;
 #pragma unroll 1
         for (int rr = 0; rr < nr; ++rr) {
-            const int row = r0 + rr;
+            const int t = g * nr + rr;
+            const int row = row_of(t);
             const int64_t h = hq ? hq[row] : 0;
-            ra_row_power<N>(x + (size_t)row * N, win, h, SQ[row], acc, accl, sm, lt, tws);
+            st.wait();
+            auto next = [&]() {
+                if (lt == 0 && t + 1 < 2 * nr) st.issue(src + (size_t)row_of(t + 1) * N, N * sizeof(float2));
+            };
+            ra_row_power<N, RAW, false>(st.buf, xw + (size_t)row * N, win, h, SQ[row], acc, accl, sm, lt, tws, next);
         }
         float* e = g ? eb : ea;
 #pragma unroll
         for (int q = 0; q < 16; ++q) {
-            const int i = fft_out_index<N>(lt, q);
+            const int i = row_out_index<N, false>(lt, q);
             const float lp = (level > 0) ? left_prev[(size_t)k * lstride * N + i] : 0.0f;
             e[i] = csum3(acc[q], accl[q], lp);
         }
@@ -379,12 +494,12 @@ k_ra_pair(const float2* __restrict__ x, const float* __restrict__ win, const int
 // (k = b / nch, chunk q = b % nch) and writes their summed |p|^2.
 template <int N>
 __global__ void __launch_bounds__(N / 16)
-k_ra_accum(const float2* __restrict__ x, const float* __restrict__ win, const int64_t* __restrict__ hq,
-           const int64_t* __restrict__ SQ, int level, int rpc, float* __restrict__ part,
-           const float2* __restrict__ tw)
+k_ra_accum(const float2* __restrict__ xw, const int64_t* __restrict__ SQ, int level, int rpc,
+           float* __restrict__ part, const float2* __restrict__ tw, unsigned* err)
 {
     using F = FFTShape<N>;
     extern __shared__ float4 dyn_smem[];
+    __shared__ __align__(8) uint64_t bar;
     float2* sm = reinterpret_cast<float2*>(dyn_smem);
     const int lt = threadIdx.x;
     const int s = 1 << level;
@@ -392,6 +507,11 @@ k_ra_accum(const float2* __restrict__ x, const float* __restrict__ win, const in
     const int k = blockIdx.x / nch, q = blockIdx.x % nch;
     const int r0 = k * s + s / 2 + q * rpc;
     float2* twt = sm + F::SMEM;
+    RowStage st{twt + RaTw<N>::kEntries, &bar, err, 0u};
+    if (lt == 0) {
+        st.init();
+        st.issue(xw + (size_t)r0 * N, N * sizeof(float2));
+    }
     RaTw<N>::fill(twt, tw, lt, F::T);
     __syncthreads();
     const RaTw<N> tws{twt};
@@ -401,11 +521,14 @@ k_ra_accum(const float2* __restrict__ x, const float* __restrict__ win, const in
 #pragma unroll 1
     for (int rr = 0; rr < rpc; ++rr) {
         const int row = r0 + rr;
-        const int64_t h = hq ? hq[row] : 0;
-        ra_row_power<N>(x + (size_t)row * N, win, h, SQ[row], acc, accl, sm, lt, tws);
+        st.wait();
+        auto next = [&]() {
+            if (lt == 0 && rr + 1 < rpc) st.issue(xw + (size_t)(row + 1) * N, N * sizeof(float2));
+        };
+        ra_row_power<N, false, true>(st.buf, nullptr, nullptr, 0, SQ[row], acc, accl, sm, lt, tws, next);
     }
 #pragma unroll
-    for (int t = 0; t < 16; ++t) part[(size_t)blockIdx.x * N + fft_out_index<N>(lt, t)] = acc[t] + accl[t];
+    for (int t = 0; t < 16; ++t) part[(size_t)blockIdx.x * N + row_out_index<N, true>(lt, t)] = acc[t] + accl[t];
 }
 
 // E[k] = left_prev[k * lstride] + sum of the nch partials of R_k
@@ -444,23 +567,30 @@ k_ra_corr(const float* __restrict__ E, double* __restrict__ S, int64_t* __restri
     for (int m = lt; m < s; m += F::T) add_shift(S, SQ, (size_t)(2 * j + 1) * s + m, sh, N);
 }
 
-// Final transform of all rows, written in place: y = IFFT(x*win*ramp)/N.
+// Final transform of all rows: y = IFFT(u * ramp) from the pre-multiplied
+// rows xw (written in place when y == xw), or with RAW (a single pulse, no
+// level ran) y = IFFT(x * win * chirp) / N from the spectra.
 // Epilogue: column sums of |y| over rows < min(M,256) per CTA (ARP partials)
 // and the global max |y| (HRRPCenter normalisation, range_alignment.cu:380-399).
-template <int N>
+template <int N, bool RAW>
 __global__ void __launch_bounds__(N / 16)
 k_ra_final(const float2* x, float2* yout, const float* __restrict__ win, const int64_t* __restrict__ hq,
            const int64_t* __restrict__ SQ, int rpc, int arp_rows, float* __restrict__ arp_part,
-           unsigned* __restrict__ hmax, const float2* __restrict__ tw)
+           unsigned* __restrict__ hmax, const float2* __restrict__ tw, unsigned* err)
 {
     using F = FFTShape<N>;
     extern __shared__ float4 dyn_smem[];
+    __shared__ __align__(8) uint64_t bar;
     float2* sm = reinterpret_cast<float2*>(dyn_smem);
     __shared__ float s_red[32];
     const int lt = threadIdx.x;
     const int r0 = blockIdx.x * rpc;
-    const float invN = 1.0f / (float)N;
     float2* twt = sm + F::SMEM;
+    RowStage st{twt + RaTw<N>::kEntries, &bar, err, 0u};
+    if (lt == 0) {
+        st.init();
+        st.issue(x + (size_t)r0 * N, N * sizeof(float2));
+    }
     RaTw<N>::fill(twt, tw, lt, F::T);
     __syncthreads();
     const RaTw<N> tws{twt};
@@ -471,27 +601,37 @@ k_ra_final(const float2* x, float2* yout, const float* __restrict__ win, const i
 #pragma unroll 1
     for (int rr = 0; rr < rpc; ++rr) {
         const int row = r0 + rr;
-        const int64_t h = hq ? hq[row] : 0;
         const int64_t sq = SQ[row];
-        const float2* xr = x + (size_t)row * N;
+        const float2* xr = st.buf;
         float2* yr = yout + (size_t)row * N;
+        st.wait();
+        auto next = [&]() {
+            if (lt == 0 && rr + 1 < rpc) st.issue(x + (size_t)(row + 1) * N, N * sizeof(float2));
+        };
         const bool arp = row < arp_rows;
-        RowPhase<N> rp;
-        rp.init(h, sq, lt);
-        team_fft<N, true>(
-            [&](int i) { return cscale(cmul(xr[i], rp.at((i - lt) / (N / 16))), __ldg(&win[i])); },
-            [&](int i, float2 v, int slot) {
-                const float2 y = make_float2(v.x * invN, v.y * invN);
-                yr[i] = y;
-                const float a = sqrtf(y.x * y.x + y.y * y.y);
-                mx = fmaxf(mx, a);
-                if (arp) acc[slot] += a;
-            },
-            sm, lt, tws);
+        auto sink = [&](int i, float2 y, int slot) {
+            yr[i] = y;
+            const float a = sqrtf(y.x * y.x + y.y * y.y);
+            mx = fmaxf(mx, a);
+            if (arp) acc[slot] += a;
+        };
+        if constexpr (RAW) {
+            const float invN = 1.0f / (float)N;
+            RowPhase<N> rp;
+            rp.init(hq ? hq[row] : 0, sq, lt);
+            row_fft<N, true, false>(
+                [&](int i) { return cscale(cmul(xr[i], rp.at((i - lt) / (N / 16))), __ldg(&win[i]) * invN); },
+                sink, sm, lt, tws, next);
+        } else {
+            LinPhase<N> lp;
+            lp.init(sq, lt);
+            row_fft<N, true, false>([&](int i) { return cmul(xr[i], lp.at((i - lt) / (N / 16))); }, sink, sm, lt, tws,
+                                    next);
+        }
     }
     if (r0 < arp_rows) {
 #pragma unroll
-        for (int t = 0; t < 16; ++t) arp_part[(size_t)blockIdx.x * N + fft_out_index<N>(lt, t)] = acc[t];
+        for (int t = 0; t < 16; ++t) arp_part[(size_t)blockIdx.x * N + row_out_index<N, false>(lt, t)] = acc[t];
     }
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
@@ -759,14 +899,18 @@ __global__ void __launch_bounds__(N / 16) k_fft_rows(float2* x, const float2* __
 // ---------------------------------------------------------------------------
 // host launchers
 // ---------------------------------------------------------------------------
+// pair correlation: FFT scratch + twiddle table + two envelopes
 template <int N>
-static size_t pair_smem()
+static size_t corr_smem()
 {
     return ((size_t)FFTShape<N>::SMEM + RaTw<N>::kEntries) * sizeof(float2) + 2 * N * sizeof(float);
 }
-// range-alignment row kernels: FFT scratch + pass twiddle tables
+// fused pair kernel: as corr_smem plus the row staging buffer
 template <int N>
-static size_t ra_fft_smem() { return ((size_t)FFTShape<N>::SMEM + RaTw<N>::kEntries) * sizeof(float2); }
+static size_t pair_smem() { return corr_smem<N>() + N * sizeof(float2); }
+// range-alignment row kernels: FFT scratch + twiddle table + row staging buffer
+template <int N>
+static size_t ra_fft_smem() { return ((size_t)FFTShape<N>::SMEM + RaTw<N>::kEntries + N) * sizeof(float2); }
 // kernels on the global twiddle table: FFT scratch only
 template <int N>
 static size_t fft_smem() { return (size_t)FFTShape<N>::SMEM * sizeof(float2); }
@@ -778,11 +922,14 @@ static cudaError_t set_attrs()
     if (done) return cudaSuccess;
     cudaError_t e;
     const int big = (int)pair_smem<N>();
-    if ((e = cudaFuncSetAttribute(k_ra_pair<N>, cudaFuncAttributeMaxDynamicSharedMemorySize, big))) return e;
-    if ((e = cudaFuncSetAttribute(k_ra_corr<N>, cudaFuncAttributeMaxDynamicSharedMemorySize, big))) return e;
+    if ((e = cudaFuncSetAttribute(k_ra_pair<N, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, big))) return e;
+    if ((e = cudaFuncSetAttribute(k_ra_pair<N, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, big))) return e;
+    if ((e = cudaFuncSetAttribute(k_ra_corr<N>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)corr_smem<N>())))
+        return e;
     const int r = (int)ra_fft_smem<N>();
     if ((e = cudaFuncSetAttribute(k_ra_accum<N>, cudaFuncAttributeMaxDynamicSharedMemorySize, r))) return e;
-    if ((e = cudaFuncSetAttribute(k_ra_final<N>, cudaFuncAttributeMaxDynamicSharedMemorySize, r))) return e;
+    if ((e = cudaFuncSetAttribute(k_ra_final<N, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, r))) return e;
+    if ((e = cudaFuncSetAttribute(k_ra_final<N, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, r))) return e;
     const int f = (int)fft_smem<N>();
     if ((e = cudaFuncSetAttribute(k_ifds_pre<N>, cudaFuncAttributeMaxDynamicSharedMemorySize, f))) return e;
     if ((e = cudaFuncSetAttribute(k_fft_rows<N, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, f))) return e;
@@ -814,8 +961,14 @@ static cudaError_t ra_run_n(const RAArgs& a, cudaStream_t st)
         const bool use_pair = (lv == 0) || pairs >= a.pair_min || (s / 2) <= 1;
         if (use_pair) {
             float* ln = last ? nullptr : bufs[cur];
-            k_ra_pair<N><<<pairs, T, pair_smem<N>(), st>>>(a.x, a.win, a.hq, a.S, a.SQ, lv, left, lstride, ln,
-                                                          a.shifts + shift_off, a.given_shifts, a.tw);
+            if (lv == 0)
+                k_ra_pair<N, true><<<pairs, T, pair_smem<N>(), st>>>(a.x, a.y, a.win, a.hq, a.S, a.SQ, lv, left,
+                                                                    lstride, ln, a.shifts + shift_off,
+                                                                    a.given_shifts, a.tw, a.err);
+            else
+                k_ra_pair<N, false><<<pairs, T, pair_smem<N>(), st>>>(a.x, a.y, a.win, a.hq, a.S, a.SQ, lv, left,
+                                                                     lstride, ln, a.shifts + shift_off,
+                                                                     a.given_shifts, a.tw, a.err);
             ISAR_COUNT(1);
             left = ln;
             lstride = 1;
@@ -824,13 +977,13 @@ static cudaError_t ra_run_n(const RAArgs& a, cudaStream_t st)
             if (rpc > s / 2) rpc = s / 2;
             const int nch = (s / 2) / rpc;
             const int groups = M / s;
-            k_ra_accum<N><<<groups * nch, T, ra_fft_smem<N>(), st>>>(a.x, a.win, a.hq, a.SQ, lv, rpc, a.part, a.tw);
+            k_ra_accum<N><<<groups * nch, T, ra_fft_smem<N>(), st>>>(a.y, a.SQ, lv, rpc, a.part, a.tw, a.err);
             ISAR_COUNT(1);
             float* E = bufs[cur];
             dim3 g((N + 255) / 256, groups);
             k_ra_reduce<<<g, 256, 0, st>>>(left, lstride, a.part, nch, N, E);
             ISAR_COUNT(1);
-            k_ra_corr<N><<<pairs, T, pair_smem<N>(), st>>>(E, a.S, a.SQ, lv, a.shifts + shift_off, a.given_shifts,
+            k_ra_corr<N><<<pairs, T, corr_smem<N>(), st>>>(E, a.S, a.SQ, lv, a.shifts + shift_off, a.given_shifts,
                                                           a.tw);
             ISAR_COUNT(1);
             left = E;
@@ -845,8 +998,12 @@ static cudaError_t ra_run_n(const RAArgs& a, cudaStream_t st)
     const int arp_rows = M < 256 ? M : 256;
     int rpcf = a.rpc_final;
     while (rpcf > 1 && (M % rpcf)) rpcf >>= 1;
-    k_ra_final<N><<<M / rpcf, T, ra_fft_smem<N>(), st>>>(a.x, a.y, a.win, a.hq, a.SQ, rpcf, arp_rows, a.part, a.hmax,
-                                                      a.tw);
+    if (L == 0)
+        k_ra_final<N, true><<<M / rpcf, T, ra_fft_smem<N>(), st>>>(a.x, a.y, a.win, a.hq, a.SQ, rpcf, arp_rows, a.part,
+                                                                  a.hmax, a.tw, a.err);
+    else
+        k_ra_final<N, false><<<M / rpcf, T, ra_fft_smem<N>(), st>>>(a.y, a.y, a.win, a.hq, a.SQ, rpcf, arp_rows,
+                                                                   a.part, a.hmax, a.tw, a.err);
     ISAR_COUNT(1);
     const int nparts = (arp_rows + rpcf - 1) / rpcf;
     k_arp_reduce<<<(N + 255) / 256, 256, 0, st>>>(a.part, nparts, N, M, a.hmax, a.arp);
