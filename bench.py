@@ -92,7 +92,7 @@ class Clocks:
     def start(self):
         try:
             self.p = subprocess.Popen(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.Q,
-                                       "--format=csv,noheader,nounits", "-lms", "200"],
+                                       "--format=csv,noheader,nounits", "-lms", "100"],
                                       stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.t = threading.Thread(target=self._read, daemon=True)
             self.t.start()
@@ -521,7 +521,7 @@ def run_profile(args):
         with g.Batch(stream=s.cuda_stream, lanes=8) as b:
             if learned:
                 b.set_warmstart(net)
-            b.set_tuning(rp, g.Tuning(ra_pair_min=128, ra_rows_per_cta=4, ra_rows_final=4, af_cluster=8,
+            b.set_tuning(rp, g.Tuning(ra_pair_min=128, ra_rows_per_cta=16, ra_rows_final=16, af_cluster=8,
                                       af_tol=TOL if learned else 0.0, af_iters=120, af_cluster_max=0))
             lst = g.Batch.frames((rp, X[i], V[i], flags, imgs[i]) for i in range(nb))
             for _ in range(args.warmup + args.steps):
@@ -536,7 +536,7 @@ def run_profile(args):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--steps", type=int, default=40)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu", action="store_true")

@@ -465,7 +465,10 @@ ISAR_API int isar_batch_set_warmstart(isar_batch* b, const isar_wsnet* net)
  * shape (isar_autotune with the cluster engine only), then the lanes per
  * shape from {1, 2, 4, 8, 16, 32} (up to the largest frame count of a shape)
  * jointly with the cluster size (16 or 8 CTAs) by timing whole-batch graph
- * replays.  The next isar_batch_run captures the chosen configuration.
+ * replays, then on the whole batch again the range-alignment rows per CTA
+ * (accumulate kernel, then final transform): with many frames in flight
+ * fewer, longer CTAs beat the single-frame choice.  The next isar_batch_run
+ * captures the chosen configuration.
  */
 ISAR_API int isar_batch_autotune(isar_batch* b, const isar_batch_frame* f, int n, float* best_ms)
 {
@@ -498,29 +501,38 @@ ISAR_API int isar_batch_autotune(isar_batch* b, const isar_batch_frame* f, int n
         s->tuning = t;
         for (auto& l : s->lanes) TRY(isar_set_tuning(l.ctx, &t));
     }
-    // lanes x cluster size on the whole batch: single-frame latency favours
-    // large clusters, concurrent lanes can favour smaller ones
-    auto apply_cluster = [&](int cl) -> int {
+    // applies fn to every shape's tuning (and its lanes)
+    auto apply = [&](auto fn) -> int {
         for (auto& sp : b->shapes) {
             Shape* s = sp.get();
-            if (cl > s->tuning.af_cluster_max) continue;
-            s->tuning.af_cluster = cl;
+            fn(s->tuning);
             for (auto& l : s->lanes) TRY(isar_set_tuning(l.ctx, &s->tuning));
         }
         return ISAR_OK;
     };
+    // whole-batch time of the current tuning with L lanes
+    auto time_with = [&](int L, float* ms) -> int {
+        BatchGraph g;
+        TRY(capture_batch(b, f, n, L, &g));
+        const int rc = time_graph(b, g.exec, 3, ms);
+        cudaGraphExecDestroy(g.exec);
+        return rc;
+    };
+    // lanes x cluster size: single-frame latency favours large clusters,
+    // concurrent lanes can favour smaller ones
+    auto set_cluster = [](int cl) {
+        return [cl](isar_tuning& t) {
+            if (cl <= t.af_cluster_max) t.af_cluster = cl;
+        };
+    };
     float best = 1e30f;
     int best_l = b->lanes, best_cl = 0;
     for (int cl : {16, 8}) {
-        TRY(apply_cluster(cl));
+        TRY(apply(set_cluster(cl)));
         for (int L : {1, 2, 4, 8, 16, 32}) {
             if (L > 1 && L / 2 >= most) break;
-            BatchGraph g;
-            TRY(capture_batch(b, f, n, L, &g));
             float ms = 0.0f;
-            const int rc = time_graph(b, g.exec, 3, &ms);
-            cudaGraphExecDestroy(g.exec);
-            TRY(rc);
+            TRY(time_with(L, &ms));
             if (ms < best) {
                 best = ms;
                 best_l = L;
@@ -528,7 +540,25 @@ ISAR_API int isar_batch_autotune(isar_batch* b, const isar_batch_frame* f, int n
             }
         }
     }
-    TRY(apply_cluster(best_cl));
+    TRY(apply(set_cluster(best_cl)));
+    // range-alignment rows per CTA at the chosen lanes (coordinate descent)
+    for (int field = 0; field < 2; ++field) {
+        auto ref = [field](isar_tuning& t) -> int& { return field == 0 ? t.ra_rows_per_cta : t.ra_rows_final; };
+        std::vector<int> orig;   // per shape, kept unless a uniform value wins
+        for (auto& sp : b->shapes) orig.push_back(ref(sp->tuning));
+        int keep = 0;
+        for (int v : {4, 8, 16, 32}) {
+            TRY(apply([&](isar_tuning& t) { ref(t) = v; }));
+            float ms = 0.0f;
+            TRY(time_with(best_l, &ms));
+            if (ms < best) {
+                best = ms;
+                keep = v;
+            }
+        }
+        size_t i = 0;
+        TRY(apply([&](isar_tuning& t) { ref(t) = keep ? keep : orig[i++]; }));
+    }
     b->lanes = best_l;
     if (best_ms) *best_ms = best;
     return ISAR_OK;

@@ -527,8 +527,18 @@ k_ra_accum(const float2* __restrict__ xw, const int64_t* __restrict__ SQ, int le
         };
         ra_row_power<N, false, true>(st.buf, nullptr, nullptr, 0, SQ[row], acc, accl, sm, lt, tws, next);
     }
+    // The warp transform leaves a lane's outputs 16 elements apart: reorder
+    // the partial sums through the scratch (one pad word every 32) so that
+    // the global stores coalesce.
+    __syncthreads();   // every warp is done with the last row's tile
+    float* pf = reinterpret_cast<float*>(sm);
 #pragma unroll
-    for (int t = 0; t < 16; ++t) part[(size_t)blockIdx.x * N + row_out_index<N, true>(lt, t)] = acc[t] + accl[t];
+    for (int t = 0; t < 16; ++t) {
+        const int i = row_out_index<N, true>(lt, t);
+        pf[i + (i >> 5)] = acc[t] + accl[t];
+    }
+    __syncthreads();
+    for (int i = lt; i < N; i += F::T) part[(size_t)blockIdx.x * N + i] = pf[i + (i >> 5)];
 }
 
 // E[k] = left_prev[k * lstride] + sum of the nch partials of R_k
