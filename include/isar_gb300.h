@@ -142,7 +142,9 @@ ISAR_API int isar_image_host(isar_ctx* ctx, const float* echo, const double* vel
  * synchronisation.  d_echo (2*M*N floats) is only read; the range profiles
  * (the reference's d_data_proc after range alignment) stay in the context,
  * see isar_get_profiles.  d_velocity: M doubles on the device (or NULL
- * without HPC).  d_img: M*512 floats.
+ * without HPC).  d_img: M*512 floats.  d_echo must be 16-byte aligned (its
+ * rows are staged into shared memory by bulk copies; cudaMalloc and torch
+ * allocations are); otherwise ISAR_EINVAL.
  */
 ISAR_API int isar_image_device(isar_ctx* ctx, const float* d_echo, const double* d_velocity, int flags, float* d_img);
 
@@ -162,7 +164,8 @@ ISAR_API int isar_get_trace(isar_ctx* ctx, isar_trace* out);
 /* highSpeedCompensation (high_speed_compensation.cu:4-54) applied to d_x. */
 ISAR_API int isar_stage_hpc(isar_ctx* ctx, float* d_x, const double* d_velocity);
 /* rangeAlignmentParallel (range_alignment.cu:4-78), with HPC fused in when
- * flags has ISAR_FLAG_HPC: spectra in d_x -> complex range profiles. */
+ * flags has ISAR_FLAG_HPC: spectra in d_x -> complex range profiles.
+ * d_x must be 16-byte aligned. */
 ISAR_API int isar_stage_range_align(isar_ctx* ctx, float* d_x, const double* d_velocity, int flags);
 /* HRRPCenter (range_alignment.cu:371-465) + cutRangeProfile
  * (common.cu:494-509): profiles d_y (M*N) -> d_cut (M*512). */
@@ -247,7 +250,7 @@ ISAR_API int isar_autotune(isar_ctx* ctx, const float* d_echo, const double* d_v
  * isar_tuning. */
 typedef struct {
     isar_radar radar;         /* M, N and radar parameters of this frame         */
-    const float* d_echo;      /* device, 2*M*N floats, read only                 */
+    const float* d_echo;      /* device, 2*M*N floats, read only, 16-byte aligned */
     const double* d_velocity; /* device, M doubles (ISAR_FLAG_HPC), or NULL      */
     int flags;                /* ISAR_FLAG_*                                     */
     float* d_img;             /* device, M*512 floats                            */
@@ -269,8 +272,9 @@ ISAR_API int isar_batch_lanes(isar_batch* b);
 /* Attaches `net` (NULL detaches) as the warm start of every lane, present
  * and future (isar_set_warmstart); drops cached graphs. */
 ISAR_API int isar_batch_set_warmstart(isar_batch* b, const isar_wsnet* net);
-/* Tunes each shape (isar_autotune, cluster engine) and the lanes per shape
- * on this frame list; *best_ms (may be NULL) = the fastest batch time. */
+/* Tunes each shape (isar_autotune, cluster engine), then on the whole frame
+ * list the lanes per shape with the cluster size, then the range-alignment
+ * rows per CTA; *best_ms (may be NULL) = the fastest batch time. */
 ISAR_API int isar_batch_autotune(isar_batch* b, const isar_batch_frame* frames, int n, float* best_ms);
 
 /* ---- learned autofocus warm start ----------------------------------------
