@@ -89,3 +89,24 @@ def test_context_autotune_cooperative_or_cluster(torch_cuda, gb300):
         assert t.af_cluster in (0, 4, 8, 16)
         got = ctx.image_host(e, v, 0)
     assert rel_l2(got, want) < TOL_RA_FREE
+
+
+def test_misaligned_echo_is_rejected_before_any_launch(torch_cuda, gb300):
+    """Rows are staged into shared memory by 16-byte bulk copies: an echo
+    buffer that is only 8-byte aligned is refused on the host (EINVAL)."""
+    torch = torch_cuda
+    M, N = 128, 512
+    base = torch.zeros(2 * M * N + 2, dtype=torch.float32, device="cuda")
+    odd = base[2:]   # 8 bytes past a 16-byte boundary
+    assert odd.data_ptr() % 16 == 8
+    vel = torch.zeros(M, dtype=torch.float64, device="cuda")
+    img = torch.zeros((M, 512), dtype=torch.float32, device="cuda")
+    rp = gb300.radar(M, N)
+    with gb300.Context(rp, stream=torch.cuda.current_stream().cuda_stream) as ctx:
+        with pytest.raises(gb300.IsarError, match="16-byte aligned"):
+            ctx.stage_range_align(odd, vel, 0)
+        with pytest.raises(gb300.IsarError, match="16-byte aligned"):
+            ctx.image_device(odd, vel, img, 0)
+    with gb300.Batch(lanes=1) as b:
+        with pytest.raises(gb300.IsarError, match="16-byte aligned"):
+            b.run(gb300.Batch.frames([(rp, odd, None, 0, img)]))
