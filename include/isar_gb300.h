@@ -324,6 +324,22 @@ ISAR_API int isar_frame_features(isar_ctx* ctx, const float* d_echo, const doubl
 /* Batched unnormalised row FFTs of length n (512..8192) in place, for tests. */
 ISAR_API int isar_fft_rows(isar_ctx* ctx, float* d_x, int rows, int n, int inverse);
 
+/* ---- IFDS ingest ----------------------------------------------------------
+ * Matched-filter pulse compression of `pulses` IFDS pulses, the
+ * reference's pulseCompression::pulseCompressionbyFFT (common.cu:635-746) as
+ * multiThreadIFDS drives it (common.cu:583-604), in one launch (one CTA per
+ * pulse).  d_ad: pulses x 2*iq_len int16 samples, I and Q interleaved
+ * (4-byte aligned); d_velocity: pulses doubles, m/s (the reference's
+ * per-pulse dataNOut entry); d_out: pulses x 4096 complex (2*4096 floats per
+ * pulse, RANGE_NUM_IFDS_PC), the 4096 cells around the maximum of each
+ * compressed pulse (cutRangeProfile, common.cu:494-509); d_offsets (may be
+ * NULL): the first cell of each cut.  B, fc, Tp and Fs come from the
+ * context's radar.  NFFT = nextPow2(iq_len) (twice iq_len for a power of
+ * two) must be 4096, 8192 or 16384, and (int)(Fs * Tp) in [2, NFFT].
+ * Stream-ordered on isar_stream(ctx). */
+ISAR_API int isar_pulse_compress(isar_ctx* ctx, const int16_t* d_ad, int iq_len, const double* d_velocity,
+                                 int pulses, float* d_out, int* d_offsets);
+
 #ifdef __cplusplus
 }
 #endif

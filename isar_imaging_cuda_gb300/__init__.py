@@ -36,7 +36,8 @@ EXPORTS = ("isar_get_last_error", "isar_version", "isar_create", "isar_destroy",
            "isar_batch_lanes", "isar_batch_autotune", "isar_wsnet_param_count", "isar_wsnet_create",
            "isar_wsnet_destroy", "isar_wsnet_stream", "isar_wsnet_set_params", "isar_wsnet_get_params",
            "isar_wsnet_forward", "isar_wsnet_backward", "isar_wsnet_get_grads", "isar_wsnet_adam",
-           "isar_nn_gemm_bf16", "isar_set_warmstart", "isar_frame_features", "isar_batch_set_warmstart")
+           "isar_nn_gemm_bf16", "isar_set_warmstart", "isar_frame_features", "isar_batch_set_warmstart",
+           "isar_pulse_compress")
 
 
 class IsarError(RuntimeError):
@@ -110,6 +111,7 @@ def load(build_if_missing=True):
         "isar_stage_fast_entropy": (i, [vp, vp, i]),
         "isar_stage_post": (i, [vp, vp, i, vp]),
         "isar_fft_rows": (i, [vp, vp, i, i, i]),
+        "isar_pulse_compress": (i, [vp, vp, i, vp, i, vp, vp]),
         "isar_get_profiles": (i, [vp, C.POINTER(vp)]),
         "isar_synth_device": (i, [C.POINTER(SynthParams), vp, vp, vp, vp]),
         "isar_launch_count": (C.c_longlong, []),
@@ -333,6 +335,14 @@ class Context:
 
     def fft_rows(self, d_x, rows, n, inverse=False):
         _check(self._lib.isar_fft_rows(self._h, _dptr(d_x), rows, n, 1 if inverse else 0), "isar_fft_rows")
+
+    def pulse_compress(self, d_ad, iq_len, d_velocity, d_out, d_offsets=None):
+        """IFDS pulse compression: d_ad int16 [P, 2*iq_len] (I, Q
+        interleaved), d_velocity float64 [P], d_out float32 [P, 4096, 2],
+        d_offsets int32 [P] or None (device tensors)."""
+        P = d_velocity.shape[0]
+        _check(self._lib.isar_pulse_compress(self._h, _dptr(d_ad), int(iq_len), _dptr(d_velocity), P,
+                                             _dptr(d_out), _dptr(d_offsets)), "isar_pulse_compress")
 
     def autotune(self, d_echo, d_velocity=None, flags=0, engines=3):
         """isar_autotune: times frames of d_echo over the launch parameters,

@@ -165,6 +165,9 @@ struct isar_ctx {
     int* d_bins = nullptr;
     float2* d_sig_part = nullptr;
     float2* d_gcol = nullptr;
+    // IFDS pulse compression: spectra of the pulses in flight (grown on demand)
+    float2* d_pc_spec = nullptr;
+    size_t pc_spec_len = 0;
     unsigned* d_bar = nullptr;     // [0] autofocus grid-barrier counter, [1] its timeout flag,
                                    // [2] range-alignment row-copy timeout flag
     // MTRC / post
@@ -842,6 +845,51 @@ ISAR_API int isar_stage_post(isar_ctx* c, float* d_cut, int flags, float* d_img)
     TRY(check_ctx(c));
     if (!d_cut || !d_img) return fail(ISAR_EINVAL, "null argument");
     CU(isar::post_run(post_args(c, reinterpret_cast<float2*>(d_cut), flags, d_img), c->st));
+    return ISAR_OK;
+}
+
+ISAR_API int isar_pulse_compress(isar_ctx* c, const int16_t* d_ad, int iq_len, const double* d_velocity,
+                                 int pulses, float* d_out, int* d_offsets)
+{
+    TRY(check_ctx(c));
+    if (!d_ad || !d_velocity || !d_out || pulses < 0 || iq_len <= 0) return fail(ISAR_EINVAL, "bad argument");
+    if ((reinterpret_cast<uintptr_t>(d_ad) & 3) || (reinterpret_cast<uintptr_t>(d_out) & 7))
+        return fail(ISAR_EINVAL, "d_ad must be 4-byte and d_out 8-byte aligned");
+    const int nfft = isar::pc_nfft(iq_len);
+    const int S = (int)((double)c->r.Fs * c->r.Tp);
+    if (nfft != 4096 && nfft != 8192 && nfft != 16384)
+        return fail(ISAR_EINVAL, "nextPow2(iq_len) = %d: supported 4096, 8192, 16384", nfft);
+    if (S < 2 || S > nfft) return fail(ISAR_EINVAL, "reference length Fs*Tp = %d outside [2, %d]", S, nfft);
+    if (pulses == 0) return ISAR_OK;
+    const size_t need = (size_t)pulses * nfft;
+    if (need > c->pc_spec_len) {
+        CU(cudaStreamSynchronize(c->st));
+        if (c->d_pc_spec) {
+            cudaFree(c->d_pc_spec);
+            c->allocs.erase(std::find(c->allocs.begin(), c->allocs.end(), (void*)c->d_pc_spec));
+            c->d_pc_spec = nullptr;
+            c->pc_spec_len = 0;
+        }
+        TRY(dalloc(c, &c->d_pc_spec, need));
+        c->pc_spec_len = need;
+    }
+    isar::PCArgs a{};
+    a.pulses = pulses;
+    a.iq_len = iq_len;
+    a.ad_stride = 2 * iq_len;
+    a.nfft = nfft;
+    a.S = S;
+    a.fc_f = (float)c->r.fc;
+    a.c2 = (float)((double)(kPiF * (float)c->r.band_width) / c->r.Tp);   // genRefPulseCompression constant_2
+    a.tp_f = (float)c->r.Tp;
+    a.ad = d_ad;
+    a.vel = d_velocity;
+    a.spec = c->d_pc_spec;
+    a.out = reinterpret_cast<float2*>(d_out);
+    a.out_stride = isar::kRangeNumIfdsPc;
+    a.offsets = d_offsets;
+    a.tw = c->d_tw;
+    CU(isar::pulse_compress(a, c->st));
     return ISAR_OK;
 }
 

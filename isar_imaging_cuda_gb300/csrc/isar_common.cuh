@@ -11,6 +11,7 @@ constexpr float kPiF = 3.14159265358979f;
 constexpr double kPiD = 3.14159265358979;
 constexpr double kLightSpeed = 300000000.0;
 constexpr int kRangeCut = 512;          // RANGE_NUM_CUT
+constexpr int kRangeNumIfdsPc = 4096;   // RANGE_NUM_IFDS_PC (common.cuh:72)
 constexpr int kEntropyIters = 120;      // FAST_ENTROPY_ITERATION_NUM
 constexpr int kMaxN = 8192;            // largest supported range_num
 constexpr int kMaxM = 1024;             // largest supported echo_num

@@ -100,6 +100,27 @@ struct PostArgs {
 cudaError_t hpc_coef(const double* vel, int M, double coef_over_fs2, int64_t* hq, cudaStream_t st);
 cudaError_t hpc_apply(float2* x, const int64_t* hq, int M, int N, cudaStream_t st);
 cudaError_t ifds_pre(float2* x, int M, int N, const float2* tw, cudaStream_t st);
+
+// IFDS pulse compression (common.cu:583-604, 635-746), one CTA per pulse.
+struct PCArgs {
+    int pulses;
+    int iq_len;              // complex samples per pulse
+    int ad_stride;           // int16 per pulse (even, >= 2 * iq_len)
+    int nfft;                // nextPow2(iq_len): 4096, 8192 or 16384
+    int S;                   // (int)(Fs * Tp) reference samples
+    float fc_f;              // (float)fc
+    float c2;                // (float)((double)(PI_FLT * (float)B) / Tp)
+    float tp_f;              // (float)Tp
+    const int16_t* ad;       // [pulses][ad_stride], I and Q interleaved
+    const double* vel;       // [pulses] m/s
+    float2* spec;            // [pulses][nfft] scratch
+    float2* out;             // [pulses][out_stride], 4096 cells each
+    int out_stride;          // float2 per output pulse
+    int* offsets;            // [pulses] cut offsets, or nullptr
+    const float2* tw;        // twiddle table exp(-2 pi i k / kTwN)
+};
+int pc_nfft(int iq_len);
+cudaError_t pulse_compress(const PCArgs& a, cudaStream_t st);
 cudaError_t ra_run(const RAArgs& a, cudaStream_t st);
 cudaError_t arp_from_y(const float2* y, int M, int N, float* tmp, unsigned* hmax, float* arp, cudaStream_t st);
 cudaError_t center_cut(const float* arp, const float2* y, int M, int N, int* dec, float2* cut, cudaStream_t st);

@@ -68,6 +68,8 @@ def lib():
         _lib.iso_cut.restype = C.c_int
         _lib.iso_next_pow2.restype = C.c_int
         _lib.iso_next_pow2.argtypes = [C.c_int]
+        _lib.iso_pulse_compress.restype = C.c_int
+        _lib.iso_pulse_compress.argtypes = [C.c_void_p, C.c_int, C.c_double, C.POINTER(Radar), C.c_void_p]
     return _lib
 
 
@@ -188,3 +190,26 @@ def post(cut, data_type=STRETCH):
     img = np.zeros((M, 512), np.float64)
     lib().iso_post(_ptr(z), M, 512, data_type, _ptr(img))
     return img
+
+
+# ---- IFDS ingest ------------------------------------------------------------
+RANGE_NUM_IFDS_PC = 4096
+
+
+def pulse_compress(ad, velocity, rp: Radar):
+    """IFDS pulse compression (common.cu:583-604, 635-746).  ad: int16
+    [P, 2*iq_len] (I, Q interleaved per pulse), velocity: [P].  Returns
+    (complex128 [P, 4096], offsets [P])."""
+    ad = np.ascontiguousarray(ad, np.int16)
+    P, two_l = ad.shape
+    out = np.zeros((P, RANGE_NUM_IFDS_PC), np.complex128)
+    offs = np.zeros(P, np.int32)
+    for p in range(P):
+        row = np.ascontiguousarray(ad[p])
+        o = np.zeros(RANGE_NUM_IFDS_PC, np.complex128)
+        r = lib().iso_pulse_compress(_ptr(row), two_l // 2, float(velocity[p]), C.byref(rp), _ptr(o))
+        if r < 0:
+            raise ValueError("pulse compression rejected (iq_len %d)" % (two_l // 2))
+        out[p] = o
+        offs[p] = r
+    return out, offs

@@ -403,6 +403,69 @@ int iso_cut(const iso_cd* x, iso_cd* cut, int M, int N, int C)
 }
 
 /* ------------------------------------------------------------------------ */
+/* IFDS ingest: per-pulse matched-filter pulse compression                   */
+/* ------------------------------------------------------------------------ */
+
+/* pulseCompression::pulseCompressionbyFFT (common.cu:635-746) for one pulse,
+ * as multiThreadIFDS drives it (common.cu:583-604): ad holds 2*iq_len int16
+ * samples (I, Q interleaved; common.cu:597-599), NFFT = nextPow2(iq_len)
+ * (Q8: 2*iq_len for a power of two), S = (int)(Fs * Tp) reference samples.
+ * Reference chirp (genTkPulseCompression, genRefPulseCompression,
+ * common.cu:620-660): tk = (1 - v2)(-Tp/2 + i Tp/(S-1)),
+ * ref = hamming_S[i] exp(j (c1 + c2 tk) tk), c1 = -2 pi fc v2/(1 - v2),
+ * c2 = pi B / Tp, v2 = 2 v / c, all in float as written (no contraction).
+ * y = IFFT(conj(FFT(ref)) .* FFT(x)) / NFFT (elementwiseMultiplyConjA,
+ * cublasCsscal), then cutRangeProfile with one row (common.cu:494-509):
+ * Icamax (|Re|+|Im|, first maximum), offset = clamp(idx - 2048, 0, NFFT - 4096),
+ * out = y[offset .. offset + 4096).  Signal arithmetic in double.
+ * Returns the offset, or -1 when NFFT < 4096 or S outside [2, NFFT]. */
+int iso_pulse_compress(const int16_t* ad, int iq_len, double velocity, const iso_radar* p, iso_cd* out)
+{
+    const int nfft = iso_next_pow2(iq_len);
+    const int S = (int)((double)p->Fs * p->Tp);
+    if (nfft < ISO_RANGE_NUM_IFDS_PC || S < 2 || S > nfft) return -1;
+    iso_cd* x = (iso_cd*)calloc((size_t)nfft, sizeof(iso_cd));
+    iso_cd* r = (iso_cd*)calloc((size_t)nfft, sizeof(iso_cd));
+    float* ham = (float*)malloc(sizeof(float) * (size_t)S);
+    for (int i = 0; i < iq_len; ++i) x[i] = (double)ad[2 * i] + I * (double)ad[2 * i + 1];
+    const float v2 = 2 * (float)velocity / (float)LIGHT_SPEED;
+    const float v2c = 1 - v2;
+    const float c1 = -2 * PI_FLT * (float)p->fc * v2 / v2c;
+    const float c2 = (float)((double)(PI_FLT * (float)p->band_width) / p->Tp);
+    const float tpf = (float)p->Tp;
+    iso_hamming_f32(ham, S);
+    for (int i = 0; i < S; ++i) {
+        const float tk = v2c * (tpf / -2.0f + (float)i * tpf / ((float)S - 1.0f));
+        const float ph = (c1 + c2 * tk) * tk;
+        const float cr = ham[i] * (float)cos((double)ph), ci = ham[i] * (float)sin((double)ph);
+        r[i] = (double)cr + I * (double)ci;
+    }
+    iso_fft(x, nfft, 0);
+    iso_fft(r, nfft, 0);
+    for (int k = 0; k < nfft; ++k) x[k] = conj(r[k]) * x[k];
+    iso_fft(x, nfft, 1);
+    const double sc = 1.0 / nfft;
+    int idx = 0;
+    double bv = -1;
+    for (int n = 0; n < nfft; ++n) {
+        x[n] *= sc;
+        const double v = fabs(creal(x[n])) + fabs(cimag(x[n]));
+        if (v > bv) {
+            bv = v;
+            idx = n;
+        }
+    }
+    int off = idx - ISO_RANGE_NUM_IFDS_PC / 2;
+    if (off < 0) off = 0;
+    if (off > nfft - ISO_RANGE_NUM_IFDS_PC) off = nfft - ISO_RANGE_NUM_IFDS_PC;
+    memcpy(out, x + off, sizeof(iso_cd) * ISO_RANGE_NUM_IFDS_PC);
+    free(x);
+    free(r);
+    free(ham);
+    return off;
+}
+
+/* ------------------------------------------------------------------------ */
 /* stage 3/4: Doppler tracking + fast entropy (phase_adjustment.cu)          */
 /* ------------------------------------------------------------------------ */
 

@@ -53,6 +53,7 @@ enum {
 };
 
 #define ISO_RANGE_NUM_CUT 512           /* common.cuh:71 */
+#define ISO_RANGE_NUM_IFDS_PC 4096      /* common.cuh:72 */
 #define ISO_ENTROPY_ITERS 120           /* common.cuh:73 */
 
 /* Discrete decisions of one frame, recorded for parity checks. */
@@ -83,6 +84,9 @@ void iso_hpc(iso_cd* x, const double* velocity, const iso_radar* p);
 void iso_range_align(iso_cd* x, const iso_radar* p, double* shifts);
 void iso_hrrp_center(iso_cd* x, const iso_radar* p, int inter_length, iso_trace* tr);
 int  iso_cut(const iso_cd* x, iso_cd* cut, int M, int N, int C);
+/* IFDS pulse compression of one pulse (common.cu:583-604, 635-746): 4096
+ * complex outputs; returns the cut offset or -1. */
+int  iso_pulse_compress(const int16_t* ad, int iq_len, double velocity, const iso_radar* p, iso_cd* out);
 void iso_doppler_tracking(iso_cd* comp, iso_cd* phase, const iso_cd* x, int M, int W, int compensate);
 void iso_fast_entropy(iso_cd* cut, int M, int C, int iters, iso_trace* tr);
 void iso_mtrc(iso_cd* cut, const iso_radar* p, int data_type);

@@ -117,6 +117,9 @@ def lib():
         _lib.ref_frame.argtypes = [C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_longlong, C.c_longlong,
                                    C.c_double, C.c_longlong, C.c_int, C.c_int, C.c_int,
                                    C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
+        _lib.ref_pulse_compress.restype = C.c_int
+        _lib.ref_pulse_compress.argtypes = [C.c_void_p, C.c_int, C.c_double, C.c_longlong, C.c_longlong,
+                                            C.c_double, C.c_longlong, C.c_void_p]
     return _lib
 
 
@@ -137,3 +140,21 @@ def frame(echo, velocity, M, N, B=1.0e9, fc=10.0e9, Fs=100.0e6, Tp=None, hpc=Fal
     if rc != 0:
         raise RuntimeError("reference rejected the frame (rc=%d)" % rc)
     return dict(img=img, ra=ra, cut=cut, fe=fe)
+
+
+def pulse_compress(ad, velocity, B, fc, Tp, Fs):
+    """IFDS pulse compression of each pulse by the reference's pulseCompression
+    class.  ad: int16 [P, 2*iq_len] (I, Q interleaved).  Returns complex64
+    [P, 4096]."""
+    ad = np.ascontiguousarray(ad, np.int16)
+    P, two_l = ad.shape
+    out = np.zeros((P, 4096), np.complex64)
+    for p in range(P):
+        iq = np.ascontiguousarray(ad[p].astype(np.float32))
+        o = np.zeros(4096, np.complex64)
+        rc = lib().ref_pulse_compress(iq.ctypes.data, two_l // 2, float(velocity[p]), int(B), int(fc), float(Tp),
+                                      int(Fs), o.ctypes.data)
+        if rc != 0:
+            raise RuntimeError("reference pulse compression failed (rc=%d)" % rc)
+        out[p] = o
+    return out

@@ -1,6 +1,7 @@
 // C entry points into the CPU-emulated reference build (TEST INFRASTRUCTURE
 // ONLY).  Compiled together with the reference's own sources; drives its
 // exported imaging path and its stage functions on host buffers.
+#include <complex>
 #include <cstring>
 #include <vector>
 
@@ -58,6 +59,26 @@ int ref_frame(const float* echo, const double* velocity, int M, int N, long long
         if (fe) std::memcpy(fe, d_data_cut, (size_t)M * 512 * sizeof(cuComplex));
     }
     imagingMemDest(data_type, b_hpc, b_hrrp);
+    return 0;
+}
+
+// One IFDS pulse through the reference's pulseCompression class, as
+// multiThreadIFDS drives it (common.cu:583-604): iq = 2*iq_len floats (the
+// int16 samples converted), out = 2*4096 floats (RANGE_NUM_IFDS_PC).
+int ref_pulse_compress(const float* iq, int iq_len, double velocity, long long band_width, long long fc, double Tp,
+                       long long Fs, float* out)
+{
+    RadarParameters p{};
+    p.band_width = band_width;
+    p.fc = fc;
+    p.Tp = Tp;
+    p.Fs = Fs;
+    pulseCompression pc(nextPow2(iq_len), iq_len, RANGE_NUM_IFDS_PC, p);
+    cuComplex* d_out = nullptr;
+    if (cudaMalloc((void**)&d_out, sizeof(cuComplex) * RANGE_NUM_IFDS_PC) != cudaSuccess) return -1;
+    pc.pulseCompressionbyFFT(d_out, reinterpret_cast<const std::complex<float>*>(iq), velocity);
+    std::memcpy(out, d_out, sizeof(cuComplex) * RANGE_NUM_IFDS_PC);
+    cudaFree(d_out);
     return 0;
 }
 

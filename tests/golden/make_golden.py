@@ -6,7 +6,9 @@ on its CPP backend, cuFFT/cuBLAS calls on double-precision stand-ins) and
 driven through its exports (imagingMemInit + isarMainSingle) on seeded
 synthetic STRETCH frames.  Each fixture stores the int16 input, the radar
 parameters and the reference's outputs: the final image and the M x 512 cut
-after HRRPCenter + cutRangeProfile.
+after HRRPCenter + cutRangeProfile.  The pc_* fixtures hold seeded IFDS pulses
+(int16 I/Q, velocities, radar parameters) and the reference's pulse
+compression of each (its pulseCompression class, 4096 cells per pulse).
 
 Run here (where the reference checkout is present):
     python tests/golden/make_golden.py
@@ -22,7 +24,7 @@ sys.path.insert(0, ROOT)
 
 import oracle  # noqa: E402
 from oracle import ref_emu  # noqa: E402
-from tests.helpers import CFG_FULL, CFG_PLAIN, full_omega  # noqa: E402
+from tests.helpers import CFG_FULL, CFG_PLAIN, PC_CASES, full_omega, make_ifds_pulses  # noqa: E402
 
 FIXTURES = {
     # name: (M, N, full pipeline (HPC + MTRC), seed)
@@ -46,6 +48,16 @@ def make(name):
     return path
 
 
+def make_pc(name, P=3, seed=7):
+    """IFDS pulse compression by the reference's pulseCompression class."""
+    iq_len, Fs, Tp, B, fc = PC_CASES[name]
+    ad, vel = make_ifds_pulses(P, iq_len, Fs, Tp, B, seed)
+    out = ref_emu.pulse_compress(ad, vel, B, fc, Tp, Fs)
+    path = os.path.join(HERE, name + ".npz")
+    np.savez_compressed(path, ad=ad, velocity=vel, iq_len=iq_len, Fs=Fs, Tp=Tp, B=B, fc=fc, out=out)
+    return path
+
+
 if __name__ == "__main__":
-    for n in sys.argv[1:] or FIXTURES:
-        print(make(n))
+    for n in sys.argv[1:] or list(FIXTURES) + list(PC_CASES):
+        print(make_pc(n) if n in PC_CASES else make(n))

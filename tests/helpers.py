@@ -29,3 +29,34 @@ def rel_l2(a, b):
     a = np.asarray(a, np.complex128)
     b = np.asarray(b, np.complex128)
     return float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300))
+
+
+# IFDS pulse-compression cases: (iq_len, Fs, Tp, B, fc); NFFT = nextPow2(iq_len)
+# is 4096, 8192 (iq_len a power of two: the doubled NFFT of nextPow2) and 16384.
+PC_CASES = {
+    "pc_4096": (3000, 100e6, 10e-6, 50e6, 10e9),
+    "pc_8192": (4096, 200e6, 10e-6, 100e6, 10e9),
+    "pc_16384": (10000, 400e6, 10e-6, 300e6, 10e9),
+}
+
+
+def make_ifds_pulses(P, iq_len, Fs, Tp, B, seed, n_scat=3, amp=800.0, noise=40.0):
+    """Seeded IFDS echoes: each pulse is the sum of n_scat delayed copies of
+    the transmitted LFM chirp (Fs*Tp samples, rate B/Tp) with random complex
+    amplitudes, plus complex Gaussian noise, as int16 [P, 2*iq_len] (I, Q
+    interleaved); velocities in m/s [P]."""
+    rng = np.random.default_rng(seed)
+    S = int(Fs * Tp)
+    t = (np.arange(S) - (S - 1) / 2.0) / Fs
+    chirp = np.exp(1j * np.pi * B / Tp * t * t)
+    ad = np.zeros((P, 2 * iq_len), np.int16)
+    for p in range(P):
+        x = (rng.normal(0, noise, iq_len) + 1j * rng.normal(0, noise, iq_len)).astype(np.complex128)
+        for _ in range(n_scat):
+            d = int(rng.integers(0, iq_len - S))
+            a = amp * rng.uniform(0.3, 1.0) * np.exp(2j * np.pi * rng.uniform())
+            x[d:d + S] += a * chirp
+        q = np.clip(np.rint(np.stack([x.real, x.imag], -1)), -32768, 32767).astype(np.int16)
+        ad[p] = q.reshape(-1)
+    vel = rng.uniform(-300.0, 300.0, P)
+    return ad, vel

@@ -166,7 +166,8 @@ def test_full_frame(torch_cuda, gb300, M, N, full, seed):
 def _goldens():
     import glob
     import os
-    return sorted(glob.glob(os.path.join(os.path.dirname(__file__), "golden", "*.npz")))
+    return sorted(p for p in glob.glob(os.path.join(os.path.dirname(__file__), "golden", "*.npz"))
+                  if not os.path.basename(p).startswith("pc_"))
 
 
 @pytest.mark.parametrize("path", _goldens(), ids=lambda p: p.rsplit("/", 1)[-1][:-4])
