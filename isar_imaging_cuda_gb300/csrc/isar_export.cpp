@@ -39,6 +39,10 @@ struct ExportState {
     int cur = -1;                          // which d_pp holds the current window
     double* d_vel = nullptr;
     float* d_img = nullptr;
+    // IFDS: raw int16 samples and per-pulse velocities of the new pulses
+    int16_t* d_ad = nullptr;
+    double* d_pcvel = nullptr;
+    size_t ad_len = 0;
 };
 
 ExportState& st()
@@ -296,8 +300,8 @@ DLL_EXPORT_API int dataExtracting(vec1D_INT* dataWFileSn, vec1D_DBL* dataNOut, v
         std::cout << "[dataExtracting/ERROR] imagingMemInit has not succeeded" << std::endl;
         return EXIT_FAILURE;
     }
-    if (data_type != ISAR_DATA_STRETCH) {
-        std::cout << "[dataExtracting/ERROR] IFDS pulse compression ingest is not supported" << std::endl;
+    if (data_type != ISAR_DATA_STRETCH && data_type != ISAR_DATA_IFDS) {
+        std::cout << "[dataExtracting/ERROR] Invalid data type!" << std::endl;
         return EXIT_FAILURE;
     }
     const int M = s.echo_num, N = s.range_num;
@@ -331,10 +335,72 @@ DLL_EXPORT_API int dataExtracting(vec1D_INT* dataWFileSn, vec1D_DBL* dataNOut, v
         std::cout << "[dataExtracting/ERROR] overlap copy failed" << std::endl;
         return EXIT_FAILURE;
     }
-    // getSignalData STRETCH branch (common.cu:1085-1106): int16 I/Q at byte 256
     std::vector<std::ifstream> ifs;
     for (const auto& p : s.files) ifs.emplace_back(p, std::ios::binary);
     const int ad_size = (frame_len - 256) / 2;
+    if (data_type == ISAR_DATA_IFDS) {
+        // getSignalData IFDS branch (common.cu:1043-1083): every new pulse's
+        // int16 samples (byte 256 on) are pulse-compressed into its row of
+        // the window (multiThreadIFDS, common.cu:583-604), here all new pulses
+        // in one launch.  Velocity of pulse i: dataNOut[echo_num +
+        // dataWFileSn[i]] as the reference indexes it (common.cu:602; the file
+        // serial number, not the window position).
+        const int iq_len = ad_size / 2;
+        std::vector<int16_t> h_ad((size_t)new_len * 2 * iq_len);
+        std::vector<double> h_v(new_len);
+        for (int i = overlap; i < M; ++i) {
+            const int sn = (*dataWFileSn)[i];
+            const int fi = sn / frame_num;
+            const size_t vi = (size_t)M + (size_t)sn;
+            if (vi >= dataNOut->size()) {
+                std::cout << "[dataExtracting/ERROR] velocity index " << vi << " beyond dataNOut ("
+                          << dataNOut->size() << ")" << std::endl;
+                return EXIT_FAILURE;
+            }
+            h_v[i - overlap] = (*dataNOut)[vi];
+            ifs[fi].seekg((std::streamoff)(sn - fi * frame_num) * frame_len + 256, std::ios::beg);
+            if (!ifs[fi].read(reinterpret_cast<char*>(h_ad.data() + (size_t)(i - overlap) * 2 * iq_len),
+                              (std::streamsize)iq_len * 4)) {
+                std::cout << "[dataExtracting/ERROR] short read in " << s.files[fi] << std::endl;
+                return EXIT_FAILURE;
+            }
+        }
+        if (h_ad.size() > s.ad_len) {
+            if (s.d_ad) cudaFree(s.d_ad);
+            if (s.d_pcvel) cudaFree(s.d_pcvel);
+            s.d_ad = nullptr;
+            s.d_pcvel = nullptr;
+            s.ad_len = 0;
+            if (cudaMalloc(&s.d_ad, h_ad.size() * sizeof(int16_t)) != cudaSuccess ||
+                cudaMalloc(&s.d_pcvel, (size_t)M * sizeof(double)) != cudaSuccess) {
+                std::cout << "[dataExtracting/ERROR] device allocation failed" << std::endl;
+                return EXIT_FAILURE;
+            }
+            s.ad_len = h_ad.size();
+        }
+        cudaStream_t cs = (cudaStream_t)isar_stream(s.ctx);
+        if (new_len > 0) {
+            if (cudaMemcpyAsync(s.d_ad, h_ad.data(), h_ad.size() * sizeof(int16_t), cudaMemcpyHostToDevice, cs) !=
+                    cudaSuccess ||
+                cudaMemcpyAsync(s.d_pcvel, h_v.data(), (size_t)new_len * sizeof(double), cudaMemcpyHostToDevice,
+                                cs) != cudaSuccess) {
+                std::cout << "[dataExtracting/ERROR] sample copy failed" << std::endl;
+                return EXIT_FAILURE;
+            }
+            if (isar_pulse_compress(s.ctx, s.d_ad, iq_len, s.d_pcvel, new_len, s.d_pp[next] + (size_t)overlap * row,
+                                    nullptr) != ISAR_OK) {
+                report("dataExtracting");
+                return EXIT_FAILURE;
+            }
+        }
+        if (cudaStreamSynchronize(cs) != cudaSuccess) {
+            std::cout << "[dataExtracting/ERROR] pulse compression failed" << std::endl;
+            return EXIT_FAILURE;
+        }
+        s.cur = next;
+        return EXIT_SUCCESS;
+    }
+    // getSignalData STRETCH branch (common.cu:1085-1106): int16 I/Q at byte 256
     std::vector<int16_t> ad(ad_size);
     for (int i = overlap; i < M; ++i) {
         const int sn = (*dataWFileSn)[i];
@@ -409,8 +475,13 @@ DLL_EXPORT_API void imagingMemDest(const int& data_type, const bool& if_hpc, con
     }
     if (s.d_vel) cudaFree(s.d_vel);
     if (s.d_img) cudaFree(s.d_img);
+    if (s.d_ad) cudaFree(s.d_ad);
+    if (s.d_pcvel) cudaFree(s.d_pcvel);
     s.d_vel = nullptr;
     s.d_img = nullptr;
+    s.d_ad = nullptr;
+    s.d_pcvel = nullptr;
+    s.ad_len = 0;
     s.cur = -1;
 }
 

@@ -2,6 +2,7 @@
 // (calling_dll.cpp:46-87) against libisar_gb300.so through the seven
 // reference exports.  Usage:
 //   dropin_main <dir> <polar_type> <window_len> <n_windows> <imaging_stride> <hpc> <mtrc> <out_prefix>
+//               [<data_type>: 2 STRETCH (default), 1 IFDS]
 // Writes <out_prefix><i>.txt per window (writeFileFLT) and prints the parsed
 // frame_len / frame_num.
 #include <cstdio>
@@ -37,7 +38,8 @@ int main(int argc, char** argv)
     int imaging_stride = std::atoi(argv[5]);
     const bool if_hpc = std::atoi(argv[6]) != 0, if_mtrc = std::atoi(argv[7]) != 0, if_hrrp = false;
     const std::string out = argv[8];
-    const int data_type = 2, sampling_stride = 1, option_alignment = 0, option_phase = 1;
+    const int data_type = argc > 9 ? std::atoi(argv[9]) : 2;
+    const int sampling_stride = 1, option_alignment = 0, option_phase = 1;
     int window_head = 0;
 
     vec1D_DBL dataN;

@@ -91,3 +91,55 @@ def test_dropin_windows_match_the_c_abi(torch_cuda, full):
             want = ctx.image_host(echo[w * stride:w * stride + M], vel[w * stride:w * stride + M], flags)
             # writeFileFLT keeps 5 decimals
             assert np.max(np.abs(got - want)) <= 6e-6 + 1e-6 * np.max(np.abs(want))
+
+
+@pytest.mark.gpu
+def test_dropin_ifds_windows_match_the_c_abi(torch_cuda):
+    """IFDS data through the seven exports: dataExtracting pulse-compresses
+    the new pulses of every window (isar_pulse_compress, one launch) with the
+    reference's velocity index dataNOut[echo_num + dataWFileSn[i]], then
+    isarMainSingle images them; equal to the C ABI path on the same pulses."""
+    from tests.helpers import make_ifds_pulses
+    torch = torch_cuda
+    exe = build_driver()
+    M, stride, nwin = 128, 32, 3
+    P = M + stride * (nwin - 1)
+    iq_len, fs, tp, B, fc = 5000, 200e6, 10e-6, 100e6, 10e9
+    ad, _ = make_ifds_pulses(P, iq_len, fs, tp, B, seed=91, n_scat=4)
+    nav_vel = np.linspace(-50.0, 50.0, P)   # navigation velocity per frame, m/s
+    d = dropin_dir(TMP, "ifds")
+    for f in os.listdir(d):
+        os.remove(os.path.join(d, f))
+    # the IFDS header stores twice the sampling rate (getSystemParas halves it)
+    write_wbd(os.path.join(d, "syn_000004_1383_01_1101.wbd"), ad.reshape(P, iq_len, 2), nav_vel, fc=fc, B=B,
+              Tp=tp, Fs=2 * fs)
+    prefix = os.path.join(d, "img_")
+    r = subprocess.run([exe, d, "1", str(M), str(nwin), str(stride), "0", "1", prefix, "1"], capture_output=True,
+                       text=True)
+    assert r.returncode == 0, r.stdout + r.stderr
+    rp = g.radar(M, 4096, B=B, fc=fc, Fs=fs, Tp=tp, data_type=g.IFDS)
+    # navigation values as dataParsing decodes them (0.1 m/s, 360/2^24 degrees)
+    dec_vel = np.round(nav_vel * 10) * 0.1
+    dec_az = np.round(np.linspace(10.0, 10.5, P) * (1 << 24) / 360.0) * (360.0 / (1 << 24))
+    dec_pit = np.round(5.0 * (1 << 24) / 360.0) * (360.0 / (1 << 24))
+    used = np.zeros(P)   # velocity each pulse was compressed with
+    with g.Context(rp, stream=torch.cuda.current_stream().cuda_stream) as ctx:
+        for w in range(nwin):
+            head = w * stride
+            sn = head + np.arange(M)
+            # dataNOut = [range, velocity, azimuth, pitching] of the window's
+            # pulses; the reference reads pulse i's velocity at M + sn_i, for
+            # the new pulses only (the overlap keeps the previous window's rows)
+            dn = np.concatenate([np.full(M, 1000.0), dec_vel[sn], dec_az[sn], np.full(M, dec_pit)])
+            new = sn[(M - stride if w else 0):]
+            used[new] = dn[M + new]
+            vel = used[sn]
+            echo = torch.zeros((M, 4096, 2), dtype=torch.float32, device="cuda")
+            ctx.pulse_compress(torch.from_numpy(ad[sn].copy()).cuda(), iq_len,
+                               torch.from_numpy(vel.copy()).cuda(), echo)
+            img = torch.zeros((M, 512), dtype=torch.float32, device="cuda")
+            ctx.image_device(echo, None, img, g.FLAG_MTRC)
+            ctx.synchronize()
+            want = img.cpu().numpy()
+            got = np.loadtxt(prefix + "%d.txt" % w).reshape(M, 512)
+            assert np.max(np.abs(got - want)) <= 6e-6 + 1e-6 * np.max(np.abs(want)), w
