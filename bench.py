@@ -361,9 +361,10 @@ def run_gb300(args):
 
 def other_workloads(g, torch, s, steps):
     """The other configurations: the plain 256 x 4096 workload (single frame
-    per call, and batches of 32 frames), and 64 frames of uneven size
-    (pulses uniform over {128, 256, 512, 1024}, range cells over
-    {2048, 4096, 8192}, plain-workload scenes) in one batch graph."""
+    per call, and batches of 32 frames), 64 frames of uneven size (pulses
+    uniform over {128, 256, 512, 1024}, range cells over {2048, 4096, 8192},
+    plain-workload scenes) in one batch graph, and the IFDS ingest's pulse
+    compression (1024 pulses of 5000 samples in one launch)."""
     import numpy as np
 
     def timed(fn, reps):
@@ -421,6 +422,22 @@ def other_workloads(g, torch, s, steps):
     out["uneven_batch64"] = {"frames_per_s": 64 * 1e3 / msu, "ms_per_batch": msu, "lanes_per_shape": lanes,
                              "shapes": len({(int(a), int(c)) for a, c in zip(Ms, Ns)}),
                              "pulse_cells": int(sum(int(a) * int(c) for a, c in zip(Ms, Ns)))}
+    del keep, frames
+    # IFDS ingest: pulse compression of 1024 pulses of 5000 samples (NFFT
+    # 8192: three 8192-point transforms per pulse) in one launch; random
+    # int16 samples (the cost does not depend on the data)
+    P, L, NF = 1024, 5000, 8192
+    rpi = g.radar(1024, 4096, B=100e6, fc=10e9, Fs=200e6, Tp=10e-6, data_type=g.IFDS)
+    gen = torch.Generator(device="cuda")
+    gen.manual_seed(11)
+    ad = torch.randint(-2000, 2000, (P, 2 * L), dtype=torch.int16, device="cuda", generator=gen)
+    vel = torch.linspace(-300.0, 300.0, P, dtype=torch.float64, device="cuda")
+    pc_out = torch.empty((P, 4096, 2), dtype=torch.float32, device="cuda")
+    with g.Context(rpi, stream=s.cuda_stream) as ctx:
+        msp = timed(lambda: ctx.pulse_compress(ad, L, vel, pc_out), max(steps, 10))
+    out["ifds_pulse_compression"] = {"pulses_per_s": P * 1e3 / msp, "ms_per_launch": msp, "pulses": P,
+                                     "iq_len": L, "nfft": NF,
+                                     "fft_gflop_per_s": P * 3 * 5 * NF * 13 / (msp * 1e-3) / 1e9}
     return out
 
 
