@@ -170,6 +170,13 @@ ISAR_API int isar_stage_range_align(isar_ctx* ctx, float* d_x, const double* d_v
 /* HRRPCenter (range_alignment.cu:371-465) + cutRangeProfile
  * (common.cu:494-509): profiles d_y (M*N) -> d_cut (M*512). */
 ISAR_API int isar_stage_center_cut(isar_ctx* ctx, const float* d_y, float* d_cut);
+/* getHRRP (common.cu:541-580): the M*N complex high-resolution range
+ * profiles of the echoes d_x into d_hrrp (may equal d_x): STRETCH rows are
+ * FFT(x * hamming) with the halves swapped, IFDS rows swap, FFT, swap.  The
+ * reference computes them when if_hrrp is set and keeps them on the device;
+ * here they are a stage of their own (the windowing that if_hrrp applies to
+ * the STRETCH echoes is ISAR_FLAG_HRRP). */
+ISAR_API int isar_stage_hrrp(isar_ctx* ctx, const float* d_x, float* d_hrrp);
 /* fastEntropy (phase_adjustment.cu:167-332) in place on d_cut. */
 ISAR_API int isar_stage_fast_entropy(isar_ctx* ctx, float* d_cut, int iterations);
 /* mtrc (mtrc.cu:4-76, when ISAR_FLAG_MTRC) and post-processing

@@ -37,7 +37,7 @@ EXPORTS = ("isar_get_last_error", "isar_version", "isar_create", "isar_destroy",
            "isar_wsnet_destroy", "isar_wsnet_stream", "isar_wsnet_set_params", "isar_wsnet_get_params",
            "isar_wsnet_forward", "isar_wsnet_backward", "isar_wsnet_get_grads", "isar_wsnet_adam",
            "isar_nn_gemm_bf16", "isar_set_warmstart", "isar_frame_features", "isar_batch_set_warmstart",
-           "isar_pulse_compress")
+           "isar_pulse_compress", "isar_stage_hrrp")
 
 
 class IsarError(RuntimeError):
@@ -112,6 +112,7 @@ def load(build_if_missing=True):
         "isar_stage_post": (i, [vp, vp, i, vp]),
         "isar_fft_rows": (i, [vp, vp, i, i, i]),
         "isar_pulse_compress": (i, [vp, vp, i, vp, i, vp, vp]),
+        "isar_stage_hrrp": (i, [vp, vp, vp]),
         "isar_get_profiles": (i, [vp, C.POINTER(vp)]),
         "isar_synth_device": (i, [C.POINTER(SynthParams), vp, vp, vp, vp]),
         "isar_launch_count": (C.c_longlong, []),
@@ -326,6 +327,9 @@ class Context:
 
     def stage_center_cut(self, d_y, d_cut):
         _check(self._lib.isar_stage_center_cut(self._h, _dptr(d_y), _dptr(d_cut)), "isar_stage_center_cut")
+
+    def stage_hrrp(self, d_x, d_hrrp):
+        _check(self._lib.isar_stage_hrrp(self._h, _dptr(d_x), _dptr(d_hrrp)), "isar_stage_hrrp")
 
     def stage_fast_entropy(self, d_cut, iterations=120):
         _check(self._lib.isar_stage_fast_entropy(self._h, _dptr(d_cut), iterations), "isar_stage_fast_entropy")

@@ -144,6 +144,7 @@ struct isar_ctx {
     // range alignment
     float* d_win = nullptr;
     float* d_win_hrrp = nullptr;   // d_win * hamming (if_hrrp on STRETCH data)
+    float* d_ham = nullptr;        // hamming(N) (getHRRP)
     int64_t* d_hq = nullptr;
     double* d_S = nullptr;
     int64_t* d_SQ = nullptr;
@@ -244,6 +245,7 @@ int build_tables(isar_ctx* c)
     hamming_f32(ham.data(), N);
     for (int n = 0; n < N; ++n) win[n] = ham[n] * (float)std::cos((double)(kPiF * (float)n));
     CU(cudaMemcpyAsync(c->d_win, win.data(), N * sizeof(float), cudaMemcpyHostToDevice, c->st));
+    CU(cudaMemcpyAsync(c->d_ham, ham.data(), N * sizeof(float), cudaMemcpyHostToDevice, c->st));
     // getHRRP windows the STRETCH echoes in place before range alignment
     // (common.cu:565): x * hamming, then x * (hamming * cos(pi n))
     std::vector<float> win_h(N);
@@ -301,6 +303,7 @@ int create_impl(isar_ctx* c)
     TRY(dalloc(c, &c->d_img, (size_t)M * C));
     TRY(dalloc(c, &c->d_win, N));
     TRY(dalloc(c, &c->d_win_hrrp, N));
+    TRY(dalloc(c, &c->d_ham, N));
     TRY(dalloc(c, &c->d_hq, M));
     TRY(dalloc(c, &c->d_S, M));
     TRY(dalloc(c, &c->d_SQ, M));
@@ -845,6 +848,15 @@ ISAR_API int isar_stage_post(isar_ctx* c, float* d_cut, int flags, float* d_img)
     TRY(check_ctx(c));
     if (!d_cut || !d_img) return fail(ISAR_EINVAL, "null argument");
     CU(isar::post_run(post_args(c, reinterpret_cast<float2*>(d_cut), flags, d_img), c->st));
+    return ISAR_OK;
+}
+
+ISAR_API int isar_stage_hrrp(isar_ctx* c, const float* d_x, float* d_hrrp)
+{
+    TRY(check_ctx(c));
+    if (!d_x || !d_hrrp) return fail(ISAR_EINVAL, "null argument");
+    CU(isar::hrrp(reinterpret_cast<const float2*>(d_x), reinterpret_cast<float2*>(d_hrrp), c->M, c->N, c->d_ham,
+                  c->r.data_type == ISAR_DATA_IFDS ? 1 : 0, c->d_tw, c->st));
     return ISAR_OK;
 }
 

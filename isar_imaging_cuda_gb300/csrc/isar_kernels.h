@@ -100,6 +100,9 @@ struct PostArgs {
 cudaError_t hpc_coef(const double* vel, int M, double coef_over_fs2, int64_t* hq, cudaStream_t st);
 cudaError_t hpc_apply(float2* x, const int64_t* hq, int M, int N, cudaStream_t st);
 cudaError_t ifds_pre(float2* x, int M, int N, const float2* tw, cudaStream_t st);
+// getHRRP (common.cu:541-580) of `rows` rows of n cells; ham = hamming(n).
+cudaError_t hrrp(const float2* x, float2* out, int rows, int n, const float* ham, int ifds, const float2* tw,
+                 cudaStream_t st);
 
 // IFDS pulse compression (common.cu:583-604, 635-746), one CTA per pulse.
 struct PCArgs {

@@ -906,6 +906,23 @@ __global__ void __launch_bounds__(N / 16) k_fft_rows(float2* x, const float2* __
     team_fft<N, INV>([&](int i) { return xr[i]; }, [&](int i, float2 v, int) { xr[i] = v; }, sm, threadIdx.x, tw);
 }
 
+// getHRRP (common.cu:541-580), one CTA per row (out may equal x): STRETCH
+// rows are FFT(x * hamming) with the halves swapped (ifftshiftRows); IFDS
+// rows are swapped, transformed and swapped again.  Both swaps are folded
+// into the transform's load and store indices.
+template <int N>
+__global__ void __launch_bounds__(N / 16)
+k_hrrp(const float2* x, float2* out, const float* __restrict__ ham, int ifds, const float2* __restrict__ tw)
+{
+    extern __shared__ float4 dyn_smem[];
+    float2* sm = reinterpret_cast<float2*>(dyn_smem);
+    const float2* xr = x + (size_t)blockIdx.x * N;
+    float2* o = out + (size_t)blockIdx.x * N;
+    team_fft<N, false>(
+        [&](int i) { return ifds ? xr[(i + N / 2) & (N - 1)] : cscale(xr[i], __ldg(&ham[i])); },
+        [&](int i, float2 v, int) { o[(i + N / 2) & (N - 1)] = v; }, sm, threadIdx.x, tw);
+}
+
 // ---------------------------------------------------------------------------
 // host launchers
 // ---------------------------------------------------------------------------
@@ -944,6 +961,7 @@ static cudaError_t set_attrs()
     if ((e = cudaFuncSetAttribute(k_ifds_pre<N>, cudaFuncAttributeMaxDynamicSharedMemorySize, f))) return e;
     if ((e = cudaFuncSetAttribute(k_fft_rows<N, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, f))) return e;
     if ((e = cudaFuncSetAttribute(k_fft_rows<N, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, f))) return e;
+    if ((e = cudaFuncSetAttribute(k_hrrp<N>, cudaFuncAttributeMaxDynamicSharedMemorySize, f))) return e;
     done = true;
     return cudaSuccess;
 }
@@ -1112,6 +1130,30 @@ static cudaError_t fftrows_n(float2* x, int rows, int inverse, const float2* tw,
     else k_fft_rows<N, false><<<rows, N / 16, fft_smem<N>(), st>>>(x, tw);
     ISAR_COUNT(1);
     return cudaGetLastError();
+}
+
+template <int N>
+static cudaError_t hrrp_n(const float2* x, float2* out, int rows, const float* ham, int ifds, const float2* tw,
+                          cudaStream_t st)
+{
+    cudaError_t e = set_attrs<N>();
+    if (e) return e;
+    k_hrrp<N><<<rows, N / 16, fft_smem<N>(), st>>>(x, out, ham, ifds, tw);
+    ISAR_COUNT(1);
+    return cudaGetLastError();
+}
+
+cudaError_t hrrp(const float2* x, float2* out, int rows, int n, const float* ham, int ifds, const float2* tw,
+                 cudaStream_t st)
+{
+    switch (n) {
+    case 512: return hrrp_n<512>(x, out, rows, ham, ifds, tw, st);
+    case 1024: return hrrp_n<1024>(x, out, rows, ham, ifds, tw, st);
+    case 2048: return hrrp_n<2048>(x, out, rows, ham, ifds, tw, st);
+    case 4096: return hrrp_n<4096>(x, out, rows, ham, ifds, tw, st);
+    case 8192: return hrrp_n<8192>(x, out, rows, ham, ifds, tw, st);
+    default: return cudaErrorInvalidValue;
+    }
 }
 
 cudaError_t fft_rows(float2* x, int rows, int n, int inverse, const float2* tw, cudaStream_t st)

@@ -68,6 +68,8 @@ def lib():
         _lib.iso_cut.restype = C.c_int
         _lib.iso_next_pow2.restype = C.c_int
         _lib.iso_next_pow2.argtypes = [C.c_int]
+        _lib.iso_hrrp.restype = None
+        _lib.iso_hrrp.argtypes = [C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_int]
         _lib.iso_pulse_compress.restype = C.c_int
         _lib.iso_pulse_compress.argtypes = [C.c_void_p, C.c_int, C.c_double, C.POINTER(Radar), C.c_void_p]
     return _lib
@@ -213,3 +215,13 @@ def pulse_compress(ad, velocity, rp: Radar):
         out[p] = o
         offs[p] = r
     return out, offs
+
+
+def hrrp(echo, data_type=STRETCH):
+    """getHRRP (common.cu:541-580): the M x N high-resolution range profiles
+    of complex echoes [M, N] (complex128 result)."""
+    x = _c128(echo)
+    M, N = x.shape
+    out = np.zeros((M, N), np.complex128)
+    lib().iso_hrrp(_ptr(x), _ptr(out), M, N, int(data_type))
+    return out

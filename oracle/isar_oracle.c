@@ -402,6 +402,28 @@ int iso_cut(const iso_cd* x, iso_cd* cut, int M, int N, int C)
     return off;
 }
 
+/* getHRRP (common.cu:541-580), the high-resolution range profiles of a
+ * frame: STRETCH: row-wise FFT of the echoes times the float range Hamming
+ * window (genHammingVec over N, which the reference applies in place),
+ * then ifftshiftRows; IFDS: ifftshiftRows, FFT, ifftshiftRows.  Rows of N
+ * (even: the shift swaps the halves). */
+void iso_hrrp(const iso_cd* x, iso_cd* out, int M, int N, int data_type)
+{
+    float* ham = (float*)malloc(sizeof(float) * (size_t)N);
+    iso_cd* row = (iso_cd*)malloc(sizeof(iso_cd) * (size_t)N);
+    iso_hamming_f32(ham, N);
+    const int h = N / 2;
+    for (int m = 0; m < M; ++m) {
+        const iso_cd* xr = x + (size_t)m * N;
+        for (int n = 0; n < N; ++n)
+            row[n] = data_type == ISO_STRETCH ? xr[n] * (double)ham[n] : xr[(n + h) % N];
+        iso_fft(row, N, 0);
+        for (int n = 0; n < N; ++n) out[(size_t)m * N + n] = row[(n + h) % N];
+    }
+    free(ham);
+    free(row);
+}
+
 /* ------------------------------------------------------------------------ */
 /* IFDS ingest: per-pulse matched-filter pulse compression                   */
 /* ------------------------------------------------------------------------ */

@@ -84,6 +84,8 @@ void iso_hpc(iso_cd* x, const double* velocity, const iso_radar* p);
 void iso_range_align(iso_cd* x, const iso_radar* p, double* shifts);
 void iso_hrrp_center(iso_cd* x, const iso_radar* p, int inter_length, iso_trace* tr);
 int  iso_cut(const iso_cd* x, iso_cd* cut, int M, int N, int C);
+/* getHRRP (common.cu:541-580): M x N range profiles of the echoes. */
+void iso_hrrp(const iso_cd* x, iso_cd* out, int M, int N, int data_type);
 /* IFDS pulse compression of one pulse (common.cu:583-604, 635-746): 4096
  * complex outputs; returns the cut offset or -1. */
 int  iso_pulse_compress(const int16_t* ad, int iq_len, double velocity, const iso_radar* p, iso_cd* out);

@@ -117,6 +117,8 @@ def lib():
         _lib.ref_frame.argtypes = [C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_longlong, C.c_longlong,
                                    C.c_double, C.c_longlong, C.c_int, C.c_int, C.c_int,
                                    C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
+        _lib.ref_hrrp.restype = C.c_int
+        _lib.ref_hrrp.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_void_p]
         _lib.ref_pulse_compress.restype = C.c_int
         _lib.ref_pulse_compress.argtypes = [C.c_void_p, C.c_int, C.c_double, C.c_longlong, C.c_longlong,
                                             C.c_double, C.c_longlong, C.c_void_p]
@@ -157,4 +159,15 @@ def pulse_compress(ad, velocity, B, fc, Tp, Fs):
         if rc != 0:
             raise RuntimeError("reference pulse compression failed (rc=%d)" % rc)
         out[p] = o
+    return out
+
+
+def hrrp(echo, data_type=2):
+    """getHRRP of a complex64 [M, N] frame by the reference (complex64 out)."""
+    e = np.ascontiguousarray(echo, np.complex64)
+    M, N = e.shape
+    out = np.zeros((M, N), np.complex64)
+    rc = lib().ref_hrrp(e.ctypes.data, M, N, int(data_type), out.ctypes.data)
+    if rc != 0:
+        raise RuntimeError("reference getHRRP failed (rc=%d)" % rc)
     return out

@@ -14,6 +14,8 @@ extern CUDAHandle handles;
 extern cuComplex* d_data_proc;
 extern cuComplex* d_data_cut;
 extern double* d_velocity;
+extern float* d_hamming;
+extern cuComplex* d_hrrp;
 
 extern "C" {
 
@@ -59,6 +61,26 @@ int ref_frame(const float* echo, const double* velocity, int M, int N, long long
         if (fe) std::memcpy(fe, d_data_cut, (size_t)M * 512 * sizeof(cuComplex));
     }
     imagingMemDest(data_type, b_hpc, b_hrrp);
+    return 0;
+}
+
+// getHRRP (common.cu:541-580) on an M x N frame through the reference's
+// imagingMemInit state (if_hrrp = true allocates d_hrrp): echo and out are
+// 2*M*N floats.
+int ref_hrrp(const float* echo, int M, int N, int data_type, float* out)
+{
+    vec1D_FLT img_v;
+    vec1D_INT sn;
+    vec1D_DBL dn;
+    vec1D_FLT ta;
+    vec1D_COM_FLT dw;
+    const int frame_len = 4 * N + 256;
+    imagingMemInit(&img_v, &sn, &dn, &ta, &dw, M, frame_len, data_type, false, true);
+    if (paras.echo_num != M || paras.range_num != N) return -2;
+    std::memcpy(d_data_proc, echo, (size_t)M * N * sizeof(cuComplex));
+    getHRRP(d_hrrp, d_data_proc, d_hamming, paras, static_cast<DATA_TYPE>(data_type), handles);
+    std::memcpy(out, d_hrrp, (size_t)M * N * sizeof(cuComplex));
+    imagingMemDest(data_type, false, true);
     return 0;
 }
 

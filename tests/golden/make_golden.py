@@ -8,7 +8,8 @@ synthetic STRETCH frames.  Each fixture stores the int16 input, the radar
 parameters and the reference's outputs: the final image and the M x 512 cut
 after HRRPCenter + cutRangeProfile.  The pc_* fixtures hold seeded IFDS pulses
 (int16 I/Q, velocities, radar parameters) and the reference's pulse
-compression of each (its pulseCompression class, 4096 cells per pulse).
+compression of each (its pulseCompression class, 4096 cells per pulse); the
+hrrp_* fixtures hold seeded int16 frames and the reference's getHRRP of them.
 
 Run here (where the reference checkout is present):
     python tests/golden/make_golden.py
@@ -58,6 +59,29 @@ def make_pc(name, P=3, seed=7):
     return path
 
 
+HRRP_CASES = {
+    # name: (M, N, data_type 2 STRETCH / 1 IFDS, seed)
+    "hrrp_stretch_16x1024": (16, 1024, 2, 31),
+    "hrrp_ifds_8x4096": (8, 4096, 1, 32),
+}
+
+
+def make_hrrp(name):
+    """getHRRP by the reference on seeded int16 I/Q frames (a few strong
+    range cells over noise)."""
+    M, N, dt, seed = HRRP_CASES[name]
+    rng = np.random.default_rng(seed)
+    x = rng.normal(0, 30, (M, N)) + 1j * rng.normal(0, 30, (M, N))
+    n = np.arange(N)
+    for _ in range(4):
+        x += 500 * np.exp(2j * np.pi * (rng.uniform(0, N) * n / N + rng.uniform()))
+    iq = np.clip(np.rint(np.stack([x.real, x.imag], -1)), -32768, 32767).astype(np.int16)
+    out = ref_emu.hrrp(oracle.iq_to_c64(iq), dt)
+    path = os.path.join(HERE, name + ".npz")
+    np.savez_compressed(path, iq=iq, data_type=dt, out=out)
+    return path
+
+
 if __name__ == "__main__":
-    for n in sys.argv[1:] or list(FIXTURES) + list(PC_CASES):
-        print(make_pc(n) if n in PC_CASES else make(n))
+    for n in sys.argv[1:] or list(FIXTURES) + list(PC_CASES) + list(HRRP_CASES):
+        print(make_pc(n) if n in PC_CASES else make_hrrp(n) if n in HRRP_CASES else make(n))

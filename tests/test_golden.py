@@ -11,8 +11,9 @@ import oracle
 from tests.helpers import rel_l2
 
 GOLDEN = sorted(p for p in glob.glob(os.path.join(os.path.dirname(__file__), "golden", "*.npz"))
-                if not os.path.basename(p).startswith("pc_"))
+                if not os.path.basename(p).startswith(("pc_", "hrrp_")))
 PC_GOLDEN = sorted(glob.glob(os.path.join(os.path.dirname(__file__), "golden", "pc_*.npz")))
+HRRP_GOLDEN = sorted(glob.glob(os.path.join(os.path.dirname(__file__), "golden", "hrrp_*.npz")))
 
 
 def load(path):
@@ -42,6 +43,16 @@ def test_oracle_matches_reference_golden(path):
 def test_goldens_present():
     assert len(GOLDEN) >= 2
     assert len(PC_GOLDEN) >= 3
+    assert len(HRRP_GOLDEN) >= 2
+
+
+@pytest.mark.parametrize("path", HRRP_GOLDEN, ids=[os.path.basename(p)[:-4] for p in HRRP_GOLDEN])
+def test_oracle_hrrp_matches_reference_golden(path):
+    """getHRRP (common.cu:541-580), STRETCH and IFDS: the oracle against the
+    reference's own getHRRP run on the CPU."""
+    z = np.load(path)
+    got = oracle.hrrp(oracle.iq_to_c64(z["iq"]), int(z["data_type"]))
+    assert rel_l2(got, z["out"]) < 1e-6
 
 
 def pc_radar(z):

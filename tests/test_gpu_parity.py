@@ -167,7 +167,7 @@ def _goldens():
     import glob
     import os
     return sorted(p for p in glob.glob(os.path.join(os.path.dirname(__file__), "golden", "*.npz"))
-                  if not os.path.basename(p).startswith("pc_"))
+                  if not os.path.basename(p).startswith(("pc_", "hrrp_")))
 
 
 @pytest.mark.parametrize("path", _goldens(), ids=lambda p: p.rsplit("/", 1)[-1][:-4])
