@@ -510,7 +510,9 @@ def run_profile(args):
     1024 x 8192 frame warmup + steps times; `batch` runs a batch of 8 frames
     through isar_batch_run with the reference algorithm (8-CTA cluster
     autofocus, 120 iterations); `learned` the same batch with the learned
-    warm start and the entropy stop criterion."""
+    warm start and the entropy stop criterion; `ifds` the IFDS pulse
+    compression of 1024 pulses of 5000 samples and the HRRP of one
+    1024 x 8192 frame."""
     import torch
 
     import isar_imaging_cuda_gb300 as g
@@ -518,7 +520,7 @@ def run_profile(args):
     torch.cuda.set_stream(s)
     rp = g.radar(M, N)
     flags = g.FLAG_HPC | g.FLAG_MTRC
-    nb = 1 if args.profile == "plain" else 8
+    nb = 8 if args.profile in ("batch", "learned") else 1
     X = torch.empty((nb, M, 2 * N), dtype=torch.float32, device="cuda")
     V = torch.empty((nb, M), dtype=torch.float64, device="cuda")
     imgs = torch.empty((nb, M, C), dtype=torch.float32, device="cuda")
@@ -529,6 +531,20 @@ def run_profile(args):
             for _ in range(args.warmup + args.steps):
                 ctx.image_device(X[0], V[0], imgs[0], flags)
             ctx.synchronize()
+    elif args.profile == "ifds":
+        P, L = 1024, 5000
+        rpi = g.radar(1024, 4096, B=100e6, fc=10e9, Fs=200e6, Tp=10e-6, data_type=g.IFDS)
+        gen = torch.Generator(device="cuda")
+        gen.manual_seed(11)
+        ad = torch.randint(-2000, 2000, (P, 2 * L), dtype=torch.int16, device="cuda", generator=gen)
+        vel = torch.linspace(-300.0, 300.0, P, dtype=torch.float64, device="cuda")
+        pc_out = torch.empty((P, 4096, 2), dtype=torch.float32, device="cuda")
+        hr = torch.empty_like(X[0])
+        with g.Context(rpi, stream=s.cuda_stream) as ci, g.Context(rp, stream=s.cuda_stream) as cs:
+            for _ in range(args.warmup + args.steps):
+                ci.pulse_compress(ad, L, vel, pc_out)
+                cs.stage_hrrp(X[0], hr)
+            ci.synchronize()
     else:
         learned = args.profile == "learned"
         net = None
@@ -557,7 +573,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu", action="store_true")
-    ap.add_argument("--profile", choices=["plain", "batch", "learned"], default=None,
+    ap.add_argument("--profile", choices=["plain", "batch", "learned", "ifds"], default=None,
                     help="run a profiling workload only (for ncu), no measurement")
     args = ap.parse_args()
     if args.profile:
