@@ -79,6 +79,7 @@ def test_cluster_stop_criterion_equals_oracle_at_same_count(torch_cuda, gb300):
         tr = ctx.trace()
     k = tr["af_iterations"]
     assert 1 <= k < 120
+    assert k % 4 == 0   # the criterion is checked every 4th iteration, before its update
     want, _ = oracle.fast_entropy(cut, iters=k)
     assert rel_l2(got, want) < TOL_IMG
 
