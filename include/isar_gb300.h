@@ -331,6 +331,14 @@ ISAR_API int isar_frame_features(isar_ctx* ctx, const float* d_echo, const doubl
 /* Batched unnormalised row FFTs of length n (512..8192) in place, for tests. */
 ISAR_API int isar_fft_rows(isar_ctx* ctx, float* d_x, int rows, int n, int inverse);
 
+/* ---- sensor samples ---------------------------------------------------------
+ * int16 I/Q pairs (the .wbd payload, I and Q interleaved) to complex64, on
+ * the device: d_iq = 2*samples int16 (8-byte aligned), d_echo = 2*samples
+ * floats (16-byte aligned), stream-ordered on `stream` (cudaStream_t or NULL).
+ * The conversion the reference's getSignalData does on the host
+ * (common.cu:1096-1098), so that a caller can move 4 bytes per sample. */
+ISAR_API int isar_iq16_to_c64(const int16_t* d_iq, float* d_echo, size_t samples, void* stream);
+
 /* ---- IFDS ingest ----------------------------------------------------------
  * Matched-filter pulse compression of `pulses` IFDS pulses, the
  * reference's pulseCompression::pulseCompressionbyFFT (common.cu:635-746) as

@@ -37,7 +37,7 @@ EXPORTS = ("isar_get_last_error", "isar_version", "isar_create", "isar_destroy",
            "isar_wsnet_destroy", "isar_wsnet_stream", "isar_wsnet_set_params", "isar_wsnet_get_params",
            "isar_wsnet_forward", "isar_wsnet_backward", "isar_wsnet_get_grads", "isar_wsnet_adam",
            "isar_nn_gemm_bf16", "isar_set_warmstart", "isar_frame_features", "isar_batch_set_warmstart",
-           "isar_pulse_compress", "isar_stage_hrrp")
+           "isar_pulse_compress", "isar_stage_hrrp", "isar_iq16_to_c64")
 
 
 class IsarError(RuntimeError):
@@ -113,6 +113,7 @@ def load(build_if_missing=True):
         "isar_fft_rows": (i, [vp, vp, i, i, i]),
         "isar_pulse_compress": (i, [vp, vp, i, vp, i, vp, vp]),
         "isar_stage_hrrp": (i, [vp, vp, vp]),
+        "isar_iq16_to_c64": (i, [vp, vp, C.c_size_t, vp]),
         "isar_get_profiles": (i, [vp, C.POINTER(vp)]),
         "isar_synth_device": (i, [C.POINTER(SynthParams), vp, vp, vp, vp]),
         "isar_launch_count": (C.c_longlong, []),
@@ -205,6 +206,16 @@ def synth_params(M, N, seed, full=False, **kw):
                  drift_sigma=0.5, phase_uniform=0.5, phase_quad=6.0, v0=3000.0, accel=50.0, snr_db=5.0)
     d.update(kw)
     return SynthParams(M=M, N=N, seed=seed, **d)
+
+
+def iq16_to_c64(d_iq, d_echo, stream=None):
+    """int16 I/Q pairs (device tensor, ... x 2) -> complex64 as float32 pairs
+    (device tensor with the same number of elements), stream-ordered."""
+    n = d_iq.numel() // 2
+    if d_echo.numel() != 2 * n:
+        raise IsarError("d_echo must hold %d floats" % (2 * n))
+    _check(load().isar_iq16_to_c64(_dptr(d_iq), _dptr(d_echo), n, C.c_void_p(stream) if stream else None),
+           "isar_iq16_to_c64")
 
 
 def synth_device(p: SynthParams, d_out, d_vel=None, stream=None, phase_err=False):

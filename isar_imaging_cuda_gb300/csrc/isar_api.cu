@@ -851,6 +851,15 @@ ISAR_API int isar_stage_post(isar_ctx* c, float* d_cut, int flags, float* d_img)
     return ISAR_OK;
 }
 
+ISAR_API int isar_iq16_to_c64(const int16_t* d_iq, float* d_echo, size_t samples, void* stream)
+{
+    if ((!d_iq || !d_echo) && samples) return fail(ISAR_EINVAL, "null argument");
+    if ((reinterpret_cast<uintptr_t>(d_iq) & 7) || (reinterpret_cast<uintptr_t>(d_echo) & 15))
+        return fail(ISAR_EINVAL, "d_iq must be 8-byte and d_echo 16-byte aligned");
+    CU(isar::iq16_to_c64(d_iq, d_echo, samples, static_cast<cudaStream_t>(stream)));
+    return ISAR_OK;
+}
+
 ISAR_API int isar_stage_hrrp(isar_ctx* c, const float* d_x, float* d_hrrp)
 {
     TRY(check_ctx(c));

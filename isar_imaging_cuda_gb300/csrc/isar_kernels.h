@@ -123,6 +123,9 @@ struct PCArgs {
     const float2* tw;        // twiddle table exp(-2 pi i k / kTwN)
 };
 int pc_nfft(int iq_len);
+// int16 I/Q pairs -> complex64 (samples complex values; in 8-byte and out
+// 16-byte aligned).
+cudaError_t iq16_to_c64(const int16_t* in, float* out, size_t samples, cudaStream_t st);
 cudaError_t pulse_compress(const PCArgs& a, cudaStream_t st);
 cudaError_t ra_run(const RAArgs& a, cudaStream_t st);
 cudaError_t arp_from_y(const float2* y, int M, int N, float* tmp, unsigned* hmax, float* arp, cudaStream_t st);

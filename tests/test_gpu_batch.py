@@ -110,3 +110,17 @@ def test_misaligned_echo_is_rejected_before_any_launch(torch_cuda, gb300):
     with gb300.Batch(lanes=1) as b:
         with pytest.raises(gb300.IsarError, match="16-byte aligned"):
             b.run(gb300.Batch.frames([(rp, odd, None, 0, img)]))
+
+
+def test_iq16_conversion_matches_the_host_cast(torch_cuda, gb300):
+    """isar_iq16_to_c64: the int16 -> float cast of getSignalData
+    (common.cu:1096-1098), done on the device; odd sample counts included."""
+    torch = torch_cuda
+    rng = np.random.default_rng(3)
+    for n in (1, 2, 7, 1000, 1 << 20):
+        iq = rng.integers(-32768, 32767, size=(n, 2), dtype=np.int16)
+        d_iq = torch.from_numpy(iq).cuda()
+        d_out = torch.full((n, 2), np.nan, dtype=torch.float32, device="cuda")
+        gb300.iq16_to_c64(d_iq, d_out, torch.cuda.current_stream().cuda_stream)
+        torch.cuda.synchronize()
+        assert np.array_equal(d_out.cpu().numpy(), iq.astype(np.float32))
