@@ -49,7 +49,11 @@ enum { ISAR_DATA_IFDS = 1, ISAR_DATA_STRETCH = 2 };
  * but on STRETCH data getHRRP multiplies the echoes in place by the range
  * Hamming window before range alignment (common.cu:565); ISAR_FLAG_HRRP
  * applies that window, so the image matches the reference's with if_hrrp. */
-enum { ISAR_FLAG_HPC = 1, ISAR_FLAG_MTRC = 2, ISAR_FLAG_HRRP = 4 };
+enum { ISAR_FLAG_HPC = 1, ISAR_FLAG_MTRC = 2, ISAR_FLAG_HRRP = 4, ISAR_FLAG_IQ16 = 8 };
+/* ISAR_FLAG_IQ16: d_echo holds the sensor's int16 I/Q samples (2*M*N int16,
+ * I and Q interleaved, as in the .wbd payload) instead of 2*M*N floats;
+ * range alignment reads them directly (the reference casts them to float on
+ * the host, common.cu:1096-1098).  Device-buffer entry points only. */
 
 /* RadarParameters (isar_imaging/common.cuh:96-117) */
 typedef struct {

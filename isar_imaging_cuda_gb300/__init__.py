@@ -20,6 +20,7 @@ IFDS = 1
 FLAG_HPC = 1
 FLAG_MTRC = 2
 FLAG_HRRP = 4
+FLAG_IQ16 = 8   # d_echo holds int16 I/Q samples (device buffers)
 RANGE_NUM_CUT = 512
 
 ISAR_OK = 0

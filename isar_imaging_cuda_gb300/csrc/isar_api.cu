@@ -423,7 +423,14 @@ int run_range_align(isar_ctx* c, const float2* x, float2* y, const double* d_vel
         CU(isar::hpc_coef(d_vel, c->M, c->hpc_coef_over_fs2, c->d_hq, c->st));
     }
     const bool hrrp = (flags & ISAR_FLAG_HRRP) && c->r.data_type == ISAR_DATA_STRETCH;
-    CU(isar::ra_run(ra_args(c, x, y, hpc, hrrp), c->st));
+    isar::RAArgs a = ra_args(c, x, y, hpc, hrrp);
+    if (flags & ISAR_FLAG_IQ16) {
+        // int16 samples: half the size of the profiles, so never in place
+        if (reinterpret_cast<const void*>(x) == reinterpret_cast<const void*>(y))
+            return fail(ISAR_EINVAL, "ISAR_FLAG_IQ16 needs separate echo and profile buffers");
+        a.x_iq16 = 1;
+    }
+    CU(isar::ra_run(a, c->st));
     return ISAR_OK;
 }
 
@@ -432,10 +439,14 @@ int run_range_align(isar_ctx* c, const float2* x, float2* y, const double* d_vel
 int run_frame_eager(isar_ctx* c, const float2* x, const double* d_vel, int flags, float* d_img)
 {
     if (c->r.data_type == ISAR_DATA_IFDS) {
-        if (x != c->d_in)
+        if (flags & ISAR_FLAG_IQ16)
+            CU(isar::iq16_to_c64(reinterpret_cast<const int16_t*>(x), reinterpret_cast<float*>(c->d_in),
+                                 (size_t)c->M * c->N, c->st));
+        else if (x != c->d_in)
             CU(cudaMemcpyAsync(c->d_in, x, (size_t)c->M * c->N * sizeof(float2), cudaMemcpyDeviceToDevice, c->st));
         CU(isar::ifds_pre(c->d_in, c->M, c->N, c->d_tw, c->st));
         x = c->d_in;
+        flags &= ~ISAR_FLAG_IQ16;
     }
     TRY(run_range_align(c, x, c->d_x, d_vel, flags));
     CU(isar::center_cut(c->d_arp, c->d_x, c->M, c->N, c->d_dec, c->d_cut, c->st));
@@ -599,6 +610,7 @@ ISAR_API int isar_image_host(isar_ctx* c, const float* echo, const double* veloc
 {
     TRY(check_ctx(c));
     if (!echo || !img) return fail(ISAR_EINVAL, "null echo/img");
+    if (flags & ISAR_FLAG_IQ16) return fail(ISAR_EINVAL, "ISAR_FLAG_IQ16 applies to device buffers only");
     const size_t MN = (size_t)c->M * c->N;
     CU(cudaMemcpyAsync(c->d_in, echo, MN * sizeof(float2), cudaMemcpyHostToDevice, c->st));
     const double* dv = nullptr;

@@ -41,6 +41,7 @@ struct RAArgs {
     int rpc_final;           // rows per CTA for the final transform
     int given_shifts;        // use the shifts already in `shifts` (test hook)
     unsigned* err;           // set when a row-copy wait runs out (rows invalid)
+    int x_iq16;              // x holds int16 I/Q pairs (level 0 reads them directly)
 };
 
 struct FEArgs {

@@ -391,7 +391,7 @@ __device__ __forceinline__ void two_sum_acc(float& s, float& c, float x)
 // (register slots of this thread).  sr: the row in the staging buffer.
 // Level 0 (raw): sr holds x, u is formed and stored to ur (global);
 // otherwise sr holds u.  hook: see team_fft.  WARP: see row_fft.
-template <int N, bool RAW, bool WARP, class Tw, class Hook>
+template <int N, bool RAW, bool WARP, bool IQ16 = false, class Tw, class Hook>
 __device__ __forceinline__ void ra_row_power(const float2* sr, float2* ur, const float* __restrict__ win, int64_t h,
                                              int64_t sq, float* acc, float* accl, float2* sm, int lt, const Tw& tw,
                                              Hook hook)
@@ -403,7 +403,14 @@ __device__ __forceinline__ void ra_row_power(const float2* sr, float2* ur, const
         rp.init(h, sq, lt);
         row_fft<N, true, WARP>(
             [&](int i) {   // i = lt + r N/16, r = 0..15 in order
-                const float2 u = cscale(cmul(sr[i], rp.at((i - lt) / (N / 16))), __ldg(&win[i]) * invN);
+                float2 xv;
+                if constexpr (IQ16) {
+                    const short2 q = reinterpret_cast<const short2*>(sr)[i];
+                    xv = make_float2((float)q.x, (float)q.y);
+                } else {
+                    xv = sr[i];
+                }
+                const float2 u = cscale(cmul(xv, rp.at((i - lt) / (N / 16))), __ldg(&win[i]) * invN);
                 ur[i] = u;   // sq = 0 at level 0: the phase is the chirp alone
                 return u;
             },
@@ -422,7 +429,7 @@ __device__ __forceinline__ void ra_row_power(const float2* sr, float2* ur, const
 // from xw and adds the carried envelopes left_prev[k] of the first halves.
 // Writes the pair shift, adds it to S of the rows of G_2j+1 and stores
 // env^2(G_2j) as left_next[j].
-template <int N, bool RAW>
+template <int N, bool RAW, bool IQ16 = false>
 __global__ void __launch_bounds__(N / 16)
 k_ra_pair(const float2* __restrict__ x, float2* xw, const float* __restrict__ win, const int64_t* __restrict__ hq,
           double* __restrict__ S, int64_t* __restrict__ SQ, int level, const float* __restrict__ left_prev,
@@ -446,11 +453,13 @@ k_ra_pair(const float2* __restrict__ x, float2* xw, const float* __restrict__ wi
         const int k = 2 * j + t / nr;
         return ((level == 0) ? k : k * s + s / 2) + t % nr;
     };
-    const float2* src = RAW ? x : xw;
+    // row r of the source: complex64 rows, or int16 I/Q rows at level 0
+    constexpr uint32_t kRowBytes = IQ16 ? N * 2 * sizeof(int16_t) : N * sizeof(float2);
+    const char* src = reinterpret_cast<const char*>(RAW ? x : xw);
     RowStage st{twt + RaTw<N>::kEntries, &bar, err, 0u};
     if (lt == 0) {
         st.init();
-        st.issue(src + (size_t)row_of(0) * N, N * sizeof(float2));
+        st.issue(src + (size_t)row_of(0) * kRowBytes, kRowBytes);
     }
     RaTw<N>::fill(twt, tw, lt, F::T);
     __syncthreads();
@@ -468,9 +477,10 @@ k_ra_pair(const float2* __restrict__ x, float2* xw, const float* __restrict__ wi
             const int64_t h = hq ? hq[row] : 0;
             st.wait();
             auto next = [&]() {
-                if (lt == 0 && t + 1 < 2 * nr) st.issue(src + (size_t)row_of(t + 1) * N, N * sizeof(float2));
+                if (lt == 0 && t + 1 < 2 * nr) st.issue(src + (size_t)row_of(t + 1) * kRowBytes, kRowBytes);
             };
-            ra_row_power<N, RAW, false>(st.buf, xw + (size_t)row * N, win, h, SQ[row], acc, accl, sm, lt, tws, next);
+            ra_row_power<N, RAW, false, IQ16>(st.buf, xw + (size_t)row * N, win, h, SQ[row], acc, accl, sm, lt, tws,
+                                              next);
         }
         float* e = g ? eb : ea;
 #pragma unroll
@@ -950,6 +960,8 @@ static cudaError_t set_attrs()
     cudaError_t e;
     const int big = (int)pair_smem<N>();
     if ((e = cudaFuncSetAttribute(k_ra_pair<N, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, big))) return e;
+    if ((e = cudaFuncSetAttribute(k_ra_pair<N, true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, big)))
+        return e;
     if ((e = cudaFuncSetAttribute(k_ra_pair<N, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, big))) return e;
     if ((e = cudaFuncSetAttribute(k_ra_corr<N>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)corr_smem<N>())))
         return e;
@@ -989,7 +1001,11 @@ static cudaError_t ra_run_n(const RAArgs& a, cudaStream_t st)
         const bool use_pair = (lv == 0) || pairs >= a.pair_min || (s / 2) <= 1;
         if (use_pair) {
             float* ln = last ? nullptr : bufs[cur];
-            if (lv == 0)
+            if (lv == 0 && a.x_iq16)
+                k_ra_pair<N, true, true><<<pairs, T, pair_smem<N>(), st>>>(a.x, a.y, a.win, a.hq, a.S, a.SQ, lv, left,
+                                                                          lstride, ln, a.shifts + shift_off,
+                                                                          a.given_shifts, a.tw, a.err);
+            else if (lv == 0)
                 k_ra_pair<N, true><<<pairs, T, pair_smem<N>(), st>>>(a.x, a.y, a.win, a.hq, a.S, a.SQ, lv, left,
                                                                     lstride, ln, a.shifts + shift_off,
                                                                     a.given_shifts, a.tw, a.err);
@@ -1026,6 +1042,7 @@ static cudaError_t ra_run_n(const RAArgs& a, cudaStream_t st)
     const int arp_rows = M < 256 ? M : 256;
     int rpcf = a.rpc_final;
     while (rpcf > 1 && (M % rpcf)) rpcf >>= 1;
+    if (L == 0 && a.x_iq16) return cudaErrorInvalidValue;   // a single pulse: no level reads x
     if (L == 0)
         k_ra_final<N, true><<<M / rpcf, T, ra_fft_smem<N>(), st>>>(a.x, a.y, a.win, a.hq, a.SQ, rpcf, arp_rows, a.part,
                                                                   a.hmax, a.tw, a.err);

@@ -124,3 +124,36 @@ def test_iq16_conversion_matches_the_host_cast(torch_cuda, gb300):
         gb300.iq16_to_c64(d_iq, d_out, torch.cuda.current_stream().cuda_stream)
         torch.cuda.synchronize()
         assert np.array_equal(d_out.cpu().numpy(), iq.astype(np.float32))
+
+
+@pytest.mark.parametrize("M,N,full,ifds", [(256, 1024, True, False), (128, 2048, False, False),
+                                           (128, 4096, False, True)])
+def test_iq16_echoes_image_like_complex64_echoes(torch_cuda, gb300, M, N, full, ifds):
+    """ISAR_FLAG_IQ16: the int16 samples read directly by range alignment (or
+    converted for the IFDS pre-step) give bit-identical images to the same
+    samples as complex64, single frame and batched."""
+    torch = torch_cuda
+    echo, vel = make_frame(M, N, seed=61, full=full)
+    iq = np.stack([echo.real, echo.imag], -1).astype(np.int16)   # the frames are int16-quantised
+    assert np.array_equal(iq.astype(np.float32), np.stack([echo.real, echo.imag], -1))
+    d_f = torch.from_numpy(np.ascontiguousarray(iq.astype(np.float32)).reshape(M, 2 * N)).cuda()
+    d_q = torch.from_numpy(np.ascontiguousarray(iq).reshape(M, 2 * N)).cuda()
+    d_v = torch.from_numpy(np.ascontiguousarray(vel, np.float64)).cuda()
+    flags = (gb300.FLAG_HPC | gb300.FLAG_MTRC) if full else 0
+    rp = gb300.radar(M, N, data_type=gb300.IFDS if ifds else gb300.STRETCH)
+    out = {}
+    with gb300.Context(rp, stream=torch.cuda.current_stream().cuda_stream) as ctx:
+        for name, x, f in (("f32", d_f, flags), ("i16", d_q, flags | gb300.FLAG_IQ16)):
+            img = torch.zeros((M, 512), dtype=torch.float32, device="cuda")
+            ctx.image_device(x, d_v, img, f)
+            ctx.image_device(x, d_v, img, f)   # second call: graph replay
+            ctx.synchronize()
+            out[name] = img.cpu().numpy()
+    assert np.array_equal(out["f32"], out["i16"])
+    if not ifds:
+        imgs = [torch.zeros((M, 512), dtype=torch.float32, device="cuda") for _ in range(2)]
+        with gb300.Batch(lanes=2) as b:
+            b.run(gb300.Batch.frames([(rp, d_q, d_v, flags | gb300.FLAG_IQ16, imgs[0]),
+                                      (rp, d_f, d_v, flags, imgs[1])]))
+            b.synchronize()
+        assert np.array_equal(imgs[0].cpu().numpy(), imgs[1].cpu().numpy())
