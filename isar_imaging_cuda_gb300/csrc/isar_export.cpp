@@ -37,6 +37,7 @@ struct ExportState {
     isar_ctx* ctx = nullptr;
     float* d_pp[2] = {nullptr, nullptr};   // ping-pong raw windows
     int cur = -1;                          // which d_pp holds the current window
+    int win_type = 0;                      // data type the windows were extracted as
     double* d_vel = nullptr;
     float* d_img = nullptr;
     // IFDS: raw int16 samples and per-pulse velocities of the new pulses
@@ -328,10 +329,19 @@ DLL_EXPORT_API int dataExtracting(vec1D_INT* dataWFileSn, vec1D_DBL* dataNOut, v
         if (overlap > M) overlap = M;
     }
     const int new_len = M - overlap;
-    const size_t row = (size_t)N * 2;   // floats per pulse
+    if (s.cur >= 0 && s.win_type != data_type) {
+        std::cout << "[dataExtracting/ERROR] data type changed between windows" << std::endl;
+        return EXIT_FAILURE;
+    }
+    s.win_type = data_type;
+    // A window row: IFDS, the 4096 complex64 cells of a compressed pulse;
+    // STRETCH, the pulse's 2N int16 I/Q samples as read (imaged with
+    // ISAR_FLAG_IQ16: half the bytes to copy and to keep).
+    const size_t row_bytes = data_type == ISAR_DATA_IFDS ? (size_t)N * 2 * sizeof(float) : (size_t)N * 2 * sizeof(int16_t);
+    char* pp_next = reinterpret_cast<char*>(s.d_pp[next]);
     if (overlap > 0 &&
-        cudaMemcpy(s.d_pp[next], s.d_pp[s.cur] + (size_t)new_len * row, (size_t)overlap * row * sizeof(float),
-                   cudaMemcpyDeviceToDevice) != cudaSuccess) {
+        cudaMemcpy(pp_next, reinterpret_cast<const char*>(s.d_pp[s.cur]) + (size_t)new_len * row_bytes,
+                   (size_t)overlap * row_bytes, cudaMemcpyDeviceToDevice) != cudaSuccess) {
         std::cout << "[dataExtracting/ERROR] overlap copy failed" << std::endl;
         return EXIT_FAILURE;
     }
@@ -387,7 +397,8 @@ DLL_EXPORT_API int dataExtracting(vec1D_INT* dataWFileSn, vec1D_DBL* dataNOut, v
                 std::cout << "[dataExtracting/ERROR] sample copy failed" << std::endl;
                 return EXIT_FAILURE;
             }
-            if (isar_pulse_compress(s.ctx, s.d_ad, iq_len, s.d_pcvel, new_len, s.d_pp[next] + (size_t)overlap * row,
+            if (isar_pulse_compress(s.ctx, s.d_ad, iq_len, s.d_pcvel, new_len,
+                                    reinterpret_cast<float*>(pp_next + (size_t)overlap * row_bytes),
                                     nullptr) != ISAR_OK) {
                 report("dataExtracting");
                 return EXIT_FAILURE;
@@ -400,22 +411,25 @@ DLL_EXPORT_API int dataExtracting(vec1D_INT* dataWFileSn, vec1D_DBL* dataNOut, v
         s.cur = next;
         return EXIT_SUCCESS;
     }
-    // getSignalData STRETCH branch (common.cu:1085-1106): int16 I/Q at byte 256
-    std::vector<int16_t> ad(ad_size);
+    // getSignalData STRETCH branch (common.cu:1085-1106): int16 I/Q at byte
+    // 256.  dataW receives the float samples as in the reference; the device
+    // window gets the int16 samples themselves.
+    std::vector<int16_t> ad((size_t)new_len * 2 * N);
     for (int i = overlap; i < M; ++i) {
         const int sn = (*dataWFileSn)[i];
         const int fi = sn / frame_num;
+        int16_t* a = ad.data() + (size_t)(i - overlap) * 2 * N;
         ifs[fi].seekg((std::streamoff)(sn - fi * frame_num) * frame_len + 256, std::ios::beg);
-        if (!ifs[fi].read(reinterpret_cast<char*>(ad.data()), (std::streamsize)ad_size * 2)) {
+        if (ad_size < 2 * N || !ifs[fi].read(reinterpret_cast<char*>(a), (std::streamsize)2 * N * 2)) {
             std::cout << "[dataExtracting/ERROR] short read in " << s.files[fi] << std::endl;
             return EXIT_FAILURE;
         }
         std::complex<float>* dst = dataW->data() + (size_t)i * N;
-        for (int j = 0; j + 1 < ad_size && j / 2 < N; j += 2) dst[j / 2] = std::complex<float>(ad[j], ad[j + 1]);
+        for (int j = 0; j < N; ++j) dst[j] = std::complex<float>(a[2 * j], a[2 * j + 1]);
     }
     if (new_len > 0 &&
-        cudaMemcpy(s.d_pp[next] + (size_t)overlap * row, dataW->data() + (size_t)overlap * N,
-                   (size_t)new_len * row * sizeof(float), cudaMemcpyHostToDevice) != cudaSuccess) {
+        cudaMemcpy(pp_next + (size_t)overlap * row_bytes, ad.data(), (size_t)new_len * row_bytes,
+                   cudaMemcpyHostToDevice) != cudaSuccess) {
         std::cout << "[dataExtracting/ERROR] echo copy failed" << std::endl;
         return EXIT_FAILURE;
     }
@@ -439,7 +453,8 @@ DLL_EXPORT_API void isarMainSingle(float* h_img, const int& data_type, const int
         return;
     }
     (void)data_type;
-    const int flags = (if_hpc ? ISAR_FLAG_HPC : 0) | (if_mtrc ? ISAR_FLAG_MTRC : 0) | (if_hrrp ? ISAR_FLAG_HRRP : 0);
+    int flags = (if_hpc ? ISAR_FLAG_HPC : 0) | (if_mtrc ? ISAR_FLAG_MTRC : 0) | (if_hrrp ? ISAR_FLAG_HRRP : 0);
+    if (s.win_type == ISAR_DATA_STRETCH) flags |= ISAR_FLAG_IQ16;   // the window holds int16 samples
     if (isar_image_device(s.ctx, s.d_pp[s.cur], s.d_vel, flags, s.d_img) != ISAR_OK) {
         report("isarMainSingle");
         return;
