@@ -16,6 +16,8 @@
 // (log2 M + 1) * M.
 #include <cuda_runtime.h>
 
+#include <type_traits>
+
 #include "fft.cuh"
 #include "isar_kernels.h"
 
@@ -760,22 +762,75 @@ k_center(const float* __restrict__ arp_g, const float2* __restrict__ y, int N, i
         srt[i] = v;
     }
     __syncthreads();
-    // bitonic sort ascending (thrust::stable_sort of arp1, :404)
-    for (int k = 2; k <= N; k <<= 1) {
-        for (int jj = k >> 1; jj > 0; jj >>= 1) {
-            for (int i = tid; i < N; i += blockDim.x) {
-                const int ixj = i ^ jj;
-                if (ixj > i) {
-                    const bool up = (i & k) == 0;
-                    const float a = srt[i], b = srt[ixj];
-                    if ((a > b) == up) {
-                        srt[i] = b;
-                        srt[ixj] = a;
+    // bitonic sort ascending (thrust::stable_sort of arp1, :404; values only,
+    // so stability does not show).  Threads t < N/8 hold elements 8t..8t+7 in
+    // registers: strides below 8 are swaps in registers, strides 8..255
+    // shuffles within a warp, and only strides of 256 and more go through
+    // shared memory (15 of the 91 stages at N = 8192).
+    {
+        const int T = N / 8;
+        const bool act = tid < T;
+        float v[8];
+        if (act) {
+#pragma unroll
+            for (int e = 0; e < 8; ++e) v[e] = srt[8 * tid + e];
+        }
+        __syncthreads();
+        for (int k = 2; k <= N; k <<= 1) {
+            for (int jj = k >> 1; jj > 0; jj >>= 1) {
+                if (jj >= 256) {
+                    if (act) {
+#pragma unroll
+                        for (int e = 0; e < 8; ++e) srt[8 * tid + e] = v[e];
                     }
+                    __syncthreads();
+                    if (act) {
+                        const int p = tid ^ (jj >> 3);
+                        const bool low = (tid & (jj >> 3)) == 0;   // element i < its partner
+#pragma unroll
+                        for (int e = 0; e < 8; ++e) {
+                            const float w = srt[8 * p + e];
+                            const bool up = ((8 * tid + e) & k) == 0;
+                            v[e] = (low == up) ? fminf(v[e], w) : fmaxf(v[e], w);
+                        }
+                    }
+                    __syncthreads();
+                } else if (jj >= 8) {
+                    if (act) {
+                        const int o = jj >> 3;
+                        const bool low = (tid & o) == 0;
+#pragma unroll
+                        for (int e = 0; e < 8; ++e) {
+                            const float w = __shfl_xor_sync(0xffffffffu, v[e], o);
+                            const bool up = ((8 * tid + e) & k) == 0;
+                            v[e] = (low == up) ? fminf(v[e], w) : fmaxf(v[e], w);
+                        }
+                    }
+                } else if (act) {
+                    // in registers; the stride as a constant keeps v[] in registers
+                    auto swaps = [&](auto J) {
+                        constexpr int jc = decltype(J)::value;
+#pragma unroll
+                        for (int e = 0; e < 8; ++e) {
+                            if ((e & jc) == 0) {
+                                const bool up = ((8 * tid + e) & k) == 0;
+                                const float a = v[e], b = v[e | jc];
+                                v[e] = up ? fminf(a, b) : fmaxf(a, b);
+                                v[e | jc] = up ? fmaxf(a, b) : fminf(a, b);
+                            }
+                        }
+                    };
+                    if (jj == 4) swaps(std::integral_constant<int, 4>{});
+                    else if (jj == 2) swaps(std::integral_constant<int, 2>{});
+                    else swaps(std::integral_constant<int, 1>{});
                 }
             }
-            __syncthreads();
         }
+        if (act) {
+#pragma unroll
+            for (int e = 0; e < 8; ++e) srt[8 * tid + e] = v[e];
+        }
+        __syncthreads();
     }
     // extra = inter_length * max(arp1) / N ; diff argmin (first index) (:406-420)
     const float arp1_max = srt[N - 1];
