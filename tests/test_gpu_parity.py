@@ -63,7 +63,10 @@ def test_hpc_stage(torch_cuda, gb300):
     assert rel_l2(got, want) < 1e-6
 
 
-@pytest.mark.parametrize("M,N,hpc", [(128, 512, False), (256, 1024, True), (256, 4096, False), (512, 2048, True)])
+# (256, 8192): the 8192-point paths (warp-level transform of the accumulate
+# kernel from level 1 on, the pair kernel at level 0, the final transform)
+@pytest.mark.parametrize("M,N,hpc", [(128, 512, False), (256, 1024, True), (256, 4096, False), (512, 2048, True),
+                                     (256, 8192, True)])
 def test_range_align_stage(torch_cuda, gb300, M, N, hpc):
     torch = torch_cuda
     e, v = make_frame(M, N, seed=M + N, full=hpc)
