@@ -389,16 +389,23 @@ __device__ __forceinline__ void two_sum_acc(float& s, float& c, float x)
 // the alignment ramp exp(-j 2 pi S n / N).  IFFT(u * ramp) is then the range
 // profile itself, with no per-element window, chirp or scaling work.
 
-// One row: IFFT(u * ramp), |.|^2 accumulated (compensated) into acc/accl
-// (register slots of this thread).  sr: the row in the staging buffer.
-// Level 0 (raw): sr holds x, u is formed and stored to ur (global);
-// otherwise sr holds u.  hook: see team_fft.  WARP: see row_fft.
-template <int N, bool RAW, bool WARP, bool IQ16 = false, class Tw, class Hook>
+// One row: IFFT(u * ramp), |.|^2 accumulated into acc/accl (register slots
+// of this thread; compensated with COMP, else a plain float sum in acc).
+// sr: the row in the staging buffer.  Level 0 (raw): sr holds x, u is formed
+// and stored to ur (global); otherwise sr holds u.  hook: see team_fft.
+// WARP: see row_fft.
+template <int N, bool RAW, bool WARP, bool IQ16 = false, bool COMP = true, class Tw, class Hook>
 __device__ __forceinline__ void ra_row_power(const float2* sr, float2* ur, const float* __restrict__ win, int64_t h,
                                              int64_t sq, float* acc, float* accl, float2* sm, int lt, const Tw& tw,
                                              Hook hook)
 {
-    auto sink = [&](int, float2 v, int slot) { two_sum_acc(acc[slot], accl[slot], v.x * v.x + v.y * v.y); };
+    auto sink = [&](int, float2 v, int slot) {
+        const float p = v.x * v.x + v.y * v.y;
+        if constexpr (COMP)
+            two_sum_acc(acc[slot], accl[slot], p);
+        else
+            acc[slot] += p;
+    };
     if constexpr (RAW) {
         const float invN = 1.0f / (float)N;
         RowPhase<N> rp;
@@ -503,7 +510,9 @@ k_ra_pair(const float2* __restrict__ x, float2* xw, const float* __restrict__ wi
 }
 
 // Level >= 1, many rows per group: CTA b transforms rpc rows of R_k
-// (k = b / nch, chunk q = b % nch) and writes their summed |p|^2.
+// (k = b / nch, chunk q = b % nch) and writes their summed |p|^2.  The sum
+// over a CTA's rows (at most 64) is a plain float sum, relative error below
+// 4e-6; k_ra_reduce adds the partials with compensation.
 template <int N>
 __global__ void __launch_bounds__(N / 16)
 k_ra_accum(const float2* __restrict__ xw, const int64_t* __restrict__ SQ, int level, int rpc,
@@ -537,7 +546,7 @@ k_ra_accum(const float2* __restrict__ xw, const int64_t* __restrict__ SQ, int le
         auto next = [&]() {
             if (lt == 0 && rr + 1 < rpc) st.issue(xw + (size_t)(row + 1) * N, N * sizeof(float2));
         };
-        ra_row_power<N, false, true>(st.buf, nullptr, nullptr, 0, SQ[row], acc, accl, sm, lt, tws, next);
+        ra_row_power<N, false, true, false, false>(st.buf, nullptr, nullptr, 0, SQ[row], acc, accl, sm, lt, tws, next);
     }
     // The warp transform leaves a lane's outputs 16 elements apart: reorder
     // the partial sums through the scratch (one pad word every 32) so that
