@@ -103,6 +103,9 @@ typedef struct {
                               /* checked every 4th iteration; cluster engine; 0 = off)*/
     int af_iters;             /* autofocus iterations, or the cap with af_tol (120)   */
     int af_cluster_max;       /* out: largest af_cluster this device can launch       */
+    int ra_rows_each_level;   /* range-alignment envelopes: 0 = spectral merge (one   */
+                              /* spectrum per group, shifted by a phase ramp); 1 =    */
+                              /* transform the shifted rows again at every level (0)  */
 } isar_tuning;
 
 typedef struct isar_ctx isar_ctx;

@@ -72,7 +72,7 @@ class Tuning(C.Structure):
     """isar_tuning: launch parameters of a context (defaults = the reference's)."""
     _fields_ = [("ra_pair_min", C.c_int), ("ra_rows_per_cta", C.c_int), ("ra_rows_final", C.c_int),
                 ("af_cluster", C.c_int), ("af_tol", C.c_float), ("af_iters", C.c_int),
-                ("af_cluster_max", C.c_int)]
+                ("af_cluster_max", C.c_int), ("ra_rows_each_level", C.c_int)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}

@@ -183,6 +183,7 @@ struct isar_ctx {
     double hpc_coef_over_fs2 = 0.0;
     bool ra_given = false;         // range alignment uses injected shifts (test hook)
     // tuning (isar_set_tuning / the autotuner); defaults as the reference
+    int ra_rows_each_level = 0;    // 0: spectral envelope merge
     int ra_pair_min = 128;
     int ra_rpc = 4;
     int ra_rpc_final = 4;
@@ -308,8 +309,10 @@ int create_impl(isar_ctx* c)
     TRY(dalloc(c, &c->d_S, M));
     TRY(dalloc(c, &c->d_SQ, M));
     TRY(dalloc(c, &c->d_shifts, M));
-    TRY(dalloc(c, &c->d_env_a, (size_t)(M / 2) * N));
-    TRY(dalloc(c, &c->d_env_b, (size_t)(M / 2) * N));
+    // env_a holds M/2 merged spectra (N complex each) or, in its two halves,
+    // the ping and pong envelopes of the carried-envelope path
+    TRY(dalloc(c, &c->d_env_a, (size_t)M * N));
+    c->d_env_b = c->d_env_a + (size_t)(M / 2) * N;
     TRY(dalloc(c, &c->d_part, (size_t)std::max(M / 2, 256) * N));
     TRY(dalloc(c, &c->d_arp, N));
     TRY(dalloc(c, &c->d_hmax, 4));
@@ -356,6 +359,7 @@ isar::RAArgs ra_args(isar_ctx* c, const float2* x, float2* y, bool hpc, bool hrr
     a.arp = c->d_arp;
     a.hmax = c->d_hmax;
     a.tw = c->d_tw;
+    a.rows_each_level = c->ra_rows_each_level;
     a.pair_min = c->ra_pair_min;
     a.rpc = c->ra_rpc;
     a.rpc_final = c->ra_rpc_final;
@@ -782,6 +786,7 @@ ISAR_API int isar_get_tuning(isar_ctx* c, isar_tuning* t)
 {
     TRY(check_ctx(c));
     if (!t) return fail(ISAR_EINVAL, "null tuning");
+    t->ra_rows_each_level = c->ra_rows_each_level;
     t->ra_pair_min = c->ra_pair_min;
     t->ra_rows_per_cta = c->ra_rpc;
     t->ra_rows_final = c->ra_rpc_final;
@@ -799,6 +804,8 @@ ISAR_API int isar_set_tuning(isar_ctx* c, const isar_tuning* t)
     if (t->ra_pair_min < 1 || !is_pow2(t->ra_rows_per_cta) || !is_pow2(t->ra_rows_final) || t->ra_rows_per_cta > 64 ||
         t->ra_rows_final > 64)
         return fail(ISAR_EINVAL, "range-alignment tuning out of range");
+    if (t->ra_rows_each_level != 0 && t->ra_rows_each_level != 1)
+        return fail(ISAR_EINVAL, "ra_rows_each_level must be 0 or 1");
     if (t->af_cluster != 0 && t->af_cluster != 4 && t->af_cluster != 8 && t->af_cluster != 16)
         return fail(ISAR_EINVAL, "af_cluster must be 0, 4, 8 or 16");
     if (t->af_cluster > isar::af_cluster_max(c->M))
@@ -809,6 +816,7 @@ ISAR_API int isar_set_tuning(isar_ctx* c, const isar_tuning* t)
     if (c->ws_w && t->af_cluster == 0) return fail(ISAR_EINVAL, "the attached warm start needs the cluster engine");
     if (t->af_iters < 0 || t->af_iters > 100000) return fail(ISAR_EINVAL, "af_iters out of range");
     CU(cudaStreamSynchronize(c->st));
+    c->ra_rows_each_level = t->ra_rows_each_level;
     c->ra_pair_min = t->ra_pair_min;
     c->ra_rpc = t->ra_rows_per_cta;
     c->ra_rpc_final = t->ra_rows_final;

@@ -311,20 +311,27 @@ ISAR_API int isar_autotune(isar_ctx* c, const float* d_echo, const double* d_vel
     best.af_tol = best.af_cluster ? base.af_tol : 0.0f;
     float best_ms = 0.0f;
     int rc = timed(best, &best_ms);
-    // coordinate descent over the range-alignment knobs, then the engine
+    // coordinate descent over the range-alignment knobs (the envelope path,
+    // then the carried-envelope path's pair threshold and rows per CTA, then
+    // the final transform's rows per CTA), then the engine
+    const int em[] = {0, 1};
     const int pm[] = {1, 8, 32, 128, 512};
     const int rp[] = {1, 2, 4, 8, 16};
     const int rf[] = {1, 2, 4, 8};
-    for (int pass = 0; pass < 4 && rc == ISAR_OK; ++pass) {
-        const int* vals = pass == 0 ? pm : pass == 1 ? rp : pass == 2 ? rf : cls.data();
-        const int nv = pass == 0 ? 5 : pass == 1 ? 5 : pass == 2 ? 4 : (int)cls.size();
+    for (int pass = 0; pass < 5 && rc == ISAR_OK; ++pass) {
+        if ((pass == 1 || pass == 2) && best.ra_rows_each_level == 0) continue;   // no effect on the spectral path
+        const int* vals = pass == 0 ? em : pass == 1 ? pm : pass == 2 ? rp : pass == 3 ? rf : cls.data();
+        const int nv = pass == 0 ? 2 : pass == 1 ? 5 : pass == 2 ? 5 : pass == 3 ? 4 : (int)cls.size();
         for (int i = 0; i < nv && rc == ISAR_OK; ++i) {
             isar_tuning t = best;
-            int* knob = pass == 0 ? &t.ra_pair_min : pass == 1 ? &t.ra_rows_per_cta : pass == 2 ? &t.ra_rows_final
-                                                                                                : &t.af_cluster;
+            int* knob = pass == 0   ? &t.ra_rows_each_level
+                        : pass == 1 ? &t.ra_pair_min
+                        : pass == 2 ? &t.ra_rows_per_cta
+                        : pass == 3 ? &t.ra_rows_final
+                                    : &t.af_cluster;
             if (*knob == vals[i]) continue;
             *knob = vals[i];
-            if (pass == 3) t.af_tol = t.af_cluster ? base.af_tol : 0.0f;
+            if (pass == 4) t.af_tol = t.af_cluster ? base.af_tol : 0.0f;
             float ms = 0.0f;
             rc = timed(t, &ms);
             if (rc == ISAR_OK && ms < best_ms) {
@@ -465,10 +472,10 @@ ISAR_API int isar_batch_set_warmstart(isar_batch* b, const isar_wsnet* net)
  * shape (isar_autotune with the cluster engine only), then the lanes per
  * shape from {1, 2, 4, 8, 16, 32} (up to the largest frame count of a shape)
  * jointly with the cluster size (16 or 8 CTAs) by timing whole-batch graph
- * replays, then on the whole batch again the range-alignment rows per CTA
- * (accumulate kernel, then final transform): with many frames in flight
- * fewer, longer CTAs beat the single-frame choice.  The next isar_batch_run
- * captures the chosen configuration.
+ * replays, then on the whole batch again the range-alignment envelope path
+ * and rows per CTA (accumulate kernel, then final transform): with many
+ * frames in flight fewer, longer CTAs beat the single-frame choice.  The next
+ * isar_batch_run captures the chosen configuration.
  */
 ISAR_API int isar_batch_autotune(isar_batch* b, const isar_batch_frame* f, int n, float* best_ms)
 {
@@ -541,13 +548,24 @@ ISAR_API int isar_batch_autotune(isar_batch* b, const isar_batch_frame* f, int n
         }
     }
     TRY(apply(set_cluster(best_cl)));
-    // range-alignment rows per CTA at the chosen lanes (coordinate descent)
-    for (int field = 0; field < 2; ++field) {
-        auto ref = [field](isar_tuning& t) -> int& { return field == 0 ? t.ra_rows_per_cta : t.ra_rows_final; };
+    // range-alignment knobs at the chosen lanes (coordinate descent): the
+    // envelope path, the accumulate kernel's rows per CTA (carried-envelope
+    // path only), the final transform's rows per CTA
+    for (int field = 0; field < 3; ++field) {
+        auto ref = [field](isar_tuning& t) -> int& {
+            return field == 0 ? t.ra_rows_each_level : field == 1 ? t.ra_rows_per_cta : t.ra_rows_final;
+        };
+        std::vector<int> vals = {4, 8, 16, 32};
+        if (field == 0) vals = {0, 1};
+        if (field == 1) {
+            bool any = false;
+            for (auto& sp : b->shapes) any = any || sp->tuning.ra_rows_each_level;
+            if (!any) continue;
+        }
         std::vector<int> orig;   // per shape, kept unless a uniform value wins
         for (auto& sp : b->shapes) orig.push_back(ref(sp->tuning));
-        int keep = 0;
-        for (int v : {4, 8, 16, 32}) {
+        int keep = -1;
+        for (int v : vals) {
             TRY(apply([&](isar_tuning& t) { ref(t) = v; }));
             float ms = 0.0f;
             TRY(time_with(best_l, &ms));
@@ -557,7 +575,10 @@ ISAR_API int isar_batch_autotune(isar_batch* b, const isar_batch_frame* f, int n
             }
         }
         size_t i = 0;
-        TRY(apply([&](isar_tuning& t) { ref(t) = keep ? keep : orig[i++]; }));
+        TRY(apply([&](isar_tuning& t) {
+            ref(t) = keep >= 0 ? keep : orig[i];
+            ++i;
+        }));
     }
     b->lanes = best_l;
     if (best_ms) *best_ms = best;

@@ -30,12 +30,14 @@ struct RAArgs {
     double* S;               // [M] cumulative alignment shift, cells
     int64_t* SQ;             // [M] S / N as a 64-bit fixed-point fraction of a cycle
     float* shifts;           // [M-1] per (level, pair) shift, level-major
-    float* env_a;            // [M/2][N] envelope ping buffer
-    float* env_b;            // [M/2][N] envelope pong buffer
-    float* part;             // [max(M/2,256)][N] partial sums
+    float* env_a;            // [M][N] envelope ping buffer; merged spectra [M/2][N] complex
+    float* env_b;            // [M/2][N] envelope pong buffer (may lie inside env_a's second half)
+    float* part;             // [max(M/2,256)][N] partial sums; merged spectra [M/4][N] complex
     float* arp;              // [N] average range profile
     unsigned* hmax;          // max |y| (float bits)
     const float2* tw;        // twiddle table exp(-2 pi i k / kTwN)
+    int rows_each_level;     // 1: transform the shifted rows at every level (carried
+                             // envelopes); 0: spectral envelope merge
     int pair_min;            // use the fused pair kernel while pairs >= pair_min
     int rpc;                 // rows per CTA for the accumulate kernel
     int rpc_final;           // rows per CTA for the final transform

@@ -301,24 +301,21 @@ __device__ __forceinline__ float csum3(float hi, float lo, float x)
 // threads).  The FFT locates the peak; the three samples of the parabola are
 // then evaluated directly, sum_n a[n] b[n - tau] with error-free float
 // accumulation, because the second difference of a broad correlation peak
-// magnifies FFT rounding into ~1e-4-cell shift errors.  ea, eb are adjacent
-// N-float shared arrays of squared envelopes; they are replaced in place by
-// the amplitudes a, b.  sm_f is the FFT scratch.
-template <int N, class Tw>
-__device__ float ra_correlate(float* ea, float* sm_f, int lt, const Tw& tw)
+// magnifies FFT rounding into ~1e-4-cell shift errors.  A(n), B(n) return
+// the amplitudes a[n], b[n] (shared-memory reads, n in [0, N)); sm_f is the
+// FFT scratch.
+template <int N, class AmpA, class AmpB, class Tw>
+__device__ float ra_correlate_f(AmpA A, AmpB B, float* sm_f, int lt, const Tw& tw)
 {
     using F = FFTShape<N>;
     constexpr int T = F::T;
     float2* sm = reinterpret_cast<float2*>(sm_f);
-    float* eb = ea + N;
     __shared__ ArgKey red[32];
     __shared__ float2 redp[32];
     __shared__ float s_res;
     __shared__ int s_pos;
-    for (int i = lt; i < 2 * N; i += T) ea[i] = sqrtf(ea[i]);
-    __syncthreads();
     // z = a + i b, forward FFT, spectrum kept in the scratch (padded slots)
-    team_fft<N, false>([&](int i) { return make_float2(ea[i], eb[i]); },
+    team_fft<N, false>([&](int i) { return make_float2(A(i), B(i)); },
                        [&](int i, float2 v, int) { sm[fpad(i)] = v; }, sm, lt, tw);
     // C[k] = A[k] * conj(B[k]) with A, B split from Z; corr = Re IFFT(C);
     // argmax over the ifftshifted index (i + N/2) mod N tracked per thread
@@ -351,9 +348,9 @@ __device__ float ra_correlate(float* ea, float* sm_f, int lt, const Tw& tw)
 #pragma unroll 4
     for (int t = 0; t < N / T; ++t) {
         const int n = lt + t * T;
-        const float a = ea[n];
+        const float a = A(n);
 #pragma unroll
-        for (int j = 0; j < 3; ++j) acc_prod(a, eb[(n - tau - (j - 1)) & (N - 1)], h[j], l[j]);
+        for (int j = 0; j < 3; ++j) acc_prod(a, B((n - tau - (j - 1)) & (N - 1)), h[j], l[j]);
     }
     double f[3];
 #pragma unroll
@@ -371,6 +368,17 @@ __device__ float ra_correlate(float* ea, float* sm_f, int lt, const Tw& tw)
     const float r = s_res;
     __syncthreads();
     return r;
+}
+
+// ra_correlate_f on squared envelopes: ea, eb are adjacent N-float shared
+// arrays, replaced in place by the amplitudes a = sqrt(ea), b = sqrt(eb).
+template <int N, class Tw>
+__device__ float ra_correlate(float* ea, float* sm_f, int lt, const Tw& tw)
+{
+    float* eb = ea + N;
+    for (int i = lt; i < 2 * N; i += FFTShape<N>::T) ea[i] = sqrtf(ea[i]);
+    __syncthreads();
+    return ra_correlate_f<N>([&](int n) { return ea[n]; }, [&](int n) { return eb[n]; }, sm_f, lt, tw);
 }
 
 // s + x accumulated error-free into (s, c) (TwoSum).
@@ -596,6 +604,180 @@ k_ra_corr(const float* __restrict__ E, double* __restrict__ S, int64_t* __restri
     const float sh = given ? shift_out[j] : shc;
     if (lt == 0 && !given) shift_out[j] = sh;
     for (int m = lt; m < s; m += F::T) add_shift(S, SQ, (size_t)(2 * j + 1) * s + m, sh, N);
+}
+
+// ---------------------------------------------------------------------------
+// Spectral envelope merge.  A row's power at half-cell spacing, w[2n] =
+// |p(n)|^2 and w[2n+1] = |p(n + 1/2)|^2, samples a trigonometric polynomial
+// whose lags lie in (-N, N) (p carries the N frequencies 0..N-1), so the
+// 2N-point spectrum W of w represents it exactly: shifting the row by s cells
+// (the reference's ramp exp(-j 2 pi k s / N) on its spectrum) multiplies W[d]
+// by exp(-j 2 pi d s / N), d the signed lag, and the power envelope of a
+// group, sum_m |p_m(n - S_m)|^2, is the even-sample inverse transform of the
+// sum of its rows' shifted spectra.  Level 0 computes each row's w (two
+// IFFTs: even and odd samples), correlates the pair and stores the merged
+// group spectrum W_a + ramp(s) W_b; every later level recovers both groups'
+// envelopes with one packed IFFT, correlates them and merges their spectra
+// with one more ramp.  Per pair that is 3 transforms instead of transforming
+// every shifted row of the group again.  w is real, so W is Hermitian and
+// only d in [0, N) is kept; W[N] is zero (p has no lag of N).
+
+// exp(-j 2 pi sq n / 2^64) slopes for LinPhase: exp(+j pi n / N) (the odd
+// samples p(n + 1/2)) and exp(-j pi n / N) (the odd half of W).
+template <int N>
+constexpr int64_t kHalfCellUp = (int64_t)(0ull - ((1ull << 63) / (uint64_t)N));
+template <int N>
+constexpr int64_t kHalfCellDown = (int64_t)((1ull << 63) / (uint64_t)N);
+
+// W[d] = E[d] + exp(-j pi d / N) O[d] from Z = FFT(w_even + j w_odd):
+// E = (Z[d] + conj Z[-d]) / 2, O = (Z[d] - conj Z[-d]) / 2j.
+__device__ __forceinline__ float2 spec_half(float2 z, float2 zm, float2 h)
+{
+    const float2 e = make_float2(0.5f * (z.x + zm.x), 0.5f * (z.y - zm.y));
+    const float2 o = make_float2(0.5f * (z.y + zm.y), -0.5f * (z.x - zm.x));
+    const float2 ho = cmul(h, o);
+    return make_float2(e.x + ho.x, e.y + ho.y);
+}
+
+// Level 0, one CTA per pair j of rows (2j, 2j+1): forms u = x * win * chirp
+// / N and stores it into xw (x may equal xw), computes both rows' half-cell
+// powers, correlates the pair, adds the shift to S of row 2j+1 and, when
+// wout is set, stores the merged spectrum W_2j + ramp(s) W_2j+1 as wout[j].
+// IQ16: x holds int16 I/Q pairs.
+template <int N, bool IQ16>
+__global__ void __launch_bounds__(N / 16)
+k_ra_spec0(const float2* x, float2* xw, const float* __restrict__ win, const int64_t* __restrict__ hq,
+           double* __restrict__ S, int64_t* __restrict__ SQ, float2* __restrict__ wout, float* shift_out, int given,
+           const float2* __restrict__ tw)
+{
+    using F = FFTShape<N>;
+    constexpr int D = N / 16;
+    extern __shared__ float4 dyn_smem[];
+    float2* sm = reinterpret_cast<float2*>(dyn_smem);
+    float2* ca = sm + F::SMEM;   // row 2j: (w[2n], w[2n+1]), then its FFT
+    float2* cb = ca + N;         // row 2j+1
+    float2* twt = cb + N;
+    const int lt = threadIdx.x, j = blockIdx.x;
+    RaTw<N>::fill(twt, tw, lt, F::T);
+    __syncthreads();
+    const RaTw<N> tws{twt};
+    const float invN = 1.0f / (float)N;
+#pragma unroll 1
+    for (int t = 0; t < 2; ++t) {
+        const int row = 2 * j + t;
+        float2* c = t ? cb : ca;
+        float2* ur = xw + (size_t)row * N;
+        RowPhase<N> rp;
+        rp.init(hq ? hq[row] : 0, 0, lt);
+        // even samples: p = IFFT(u); each thread reads, then overwrites, its
+        // own elements of x (in place when x == xw)
+        team_fft<N, true>(
+            [&](int i) {
+                float2 xv;
+                if constexpr (IQ16) {
+                    const short2 q = reinterpret_cast<const short2*>(x)[(size_t)row * N + i];
+                    xv = make_float2((float)q.x, (float)q.y);
+                } else {
+                    xv = x[(size_t)row * N + i];
+                }
+                const float2 u = cscale(cmul(xv, rp.at((i - lt) / D)), __ldg(&win[i]) * invN);
+                ur[i] = u;
+                return u;
+            },
+            [&](int n, float2 v, int) { c[n].x = v.x * v.x + v.y * v.y; }, sm, lt, tws);
+        // odd samples: p(n + 1/2) = IFFT(u * exp(j pi k / N)); the thread
+        // reads back the u it stored itself
+        LinPhase<N> hp;
+        hp.init(kHalfCellUp<N>, lt);
+        team_fft<N, true>([&](int i) { return cmul(ur[i], hp.at((i - lt) / D)); },
+                          [&](int n, float2 v, int) { c[n].y = v.x * v.x + v.y * v.y; }, sm, lt, tws);
+    }
+    __syncthreads();
+    const float shc = ra_correlate_f<N>([&](int n) { return sqrtf(ca[n].x); }, [&](int n) { return sqrtf(cb[n].x); },
+                                        reinterpret_cast<float*>(sm), lt, tws);
+    const float sh = given ? shift_out[j] : shc;   // given: shifts injected by the caller (test hook)
+    if (lt == 0) {
+        if (!given) shift_out[j] = sh;
+        add_shift(S, SQ, (size_t)2 * j + 1, sh, N);
+    }
+    if (wout == nullptr) return;
+    // Z = FFT(w_even + j w_odd) in place (team_fft reads all its inputs
+    // before its first barrier and writes its outputs after the last)
+    team_fft<N, false>([&](int i) { return ca[i]; }, [&](int k, float2 v, int) { ca[k] = v; }, sm, lt, tws);
+    team_fft<N, false>([&](int i) { return cb[i]; }, [&](int k, float2 v, int) { cb[k] = v; }, sm, lt, tws);
+    __syncthreads();
+    LinPhase<N> h, r;
+    h.init(kHalfCellDown<N>, lt);
+    r.init(frac_to_fixed((double)sh / (double)N), lt);
+    float2* w = wout + (size_t)j * N;
+#pragma unroll
+    for (int q = 0; q < 16; ++q) {
+        const int d = lt + q * D;
+        const int dm = (N - d) & (N - 1);
+        const float2 hd = h.at(q), rd = r.at(q);
+        const float2 wa = spec_half(ca[d], ca[dm], hd);
+        const float2 wb = cmul(rd, spec_half(cb[d], cb[dm], hd));
+        w[d] = make_float2(wa.x + wb.x, wa.y + wb.y);
+    }
+}
+
+// Level >= 1, one CTA per pair j of groups (G_2j, G_2j+1) with merged
+// spectra wprev[2j], wprev[2j+1]: envelopes
+// env_a + j env_b = IFFT(X_a + j X_b) / (2N), X[d] = W[d] + conj W[N - d],
+// correlation, the shift added to S of the rows of G_2j+1 and, when wout is
+// set, the merged spectrum W_2j + ramp(s) W_2j+1 stored as wout[j].
+template <int N>
+__global__ void __launch_bounds__(N / 16)
+k_ra_spec(const float2* __restrict__ wprev, float2* __restrict__ wout, double* __restrict__ S,
+          int64_t* __restrict__ SQ, int level, float* shift_out, int given, const float2* __restrict__ tw)
+{
+    using F = FFTShape<N>;
+    constexpr int D = N / 16;
+    extern __shared__ float4 dyn_smem[];
+    float* sm_f = reinterpret_cast<float*>(dyn_smem);
+    float* ea = sm_f + 2 * F::SMEM;
+    float* eb = ea + N;
+    float2* twt = reinterpret_cast<float2*>(eb + N);
+    float2* sm = reinterpret_cast<float2*>(sm_f);
+    const int lt = threadIdx.x, j = blockIdx.x;
+    const int s = 1 << level;
+    RaTw<N>::fill(twt, tw, lt, F::T);
+    __syncthreads();
+    const RaTw<N> tws{twt};
+    const float2* wa = wprev + (size_t)2 * j * N;
+    const float2* wb = wa + N;
+    const float inv2N = 0.5f / (float)N;
+    team_fft<N, true>(
+        [&](int d) {
+            float2 xa = __ldg(&wa[d]), xb = __ldg(&wb[d]);
+            if (d) {
+                const float2 am = __ldg(&wa[N - d]), bm = __ldg(&wb[N - d]);
+                xa = make_float2(xa.x + am.x, xa.y - am.y);
+                xb = make_float2(xb.x + bm.x, xb.y - bm.y);
+            }
+            return make_float2(xa.x - xb.y, xa.y + xb.x);
+        },
+        [&](int n, float2 v, int) {
+            ea[n] = sqrtf(fmaxf(v.x * inv2N, 0.0f));
+            eb[n] = sqrtf(fmaxf(v.y * inv2N, 0.0f));
+        },
+        sm, lt, tws);
+    __syncthreads();
+    const float shc = ra_correlate_f<N>([&](int n) { return ea[n]; }, [&](int n) { return eb[n]; }, sm_f, lt, tws);
+    const float sh = given ? shift_out[j] : shc;
+    if (lt == 0 && !given) shift_out[j] = sh;
+    for (int m = lt; m < s; m += F::T) add_shift(S, SQ, (size_t)(2 * j + 1) * s + m, sh, N);
+    if (wout == nullptr) return;
+    LinPhase<N> r;
+    r.init(frac_to_fixed((double)sh / (double)N), lt);
+    float2* w = wout + (size_t)j * N;
+#pragma unroll
+    for (int q = 0; q < 16; ++q) {
+        const int d = lt + q * D;
+        const float2 rb = cmul(r.at(q), __ldg(&wb[d]));
+        const float2 a = __ldg(&wa[d]);
+        w[d] = make_float2(a.x + rb.x, a.y + rb.y);
+    }
 }
 
 // Final transform of all rows: y = IFFT(u * ramp) from the pre-multiplied
@@ -1009,6 +1191,9 @@ static size_t corr_smem()
 // fused pair kernel: as corr_smem plus the row staging buffer
 template <int N>
 static size_t pair_smem() { return corr_smem<N>() + N * sizeof(float2); }
+// spectral level 0: FFT scratch + two rows of half-cell powers + twiddle table
+template <int N>
+static size_t spec0_smem() { return ((size_t)FFTShape<N>::SMEM + 2 * N + RaTw<N>::kEntries) * sizeof(float2); }
 // range-alignment row kernels: FFT scratch + twiddle table + row staging buffer
 template <int N>
 static size_t ra_fft_smem() { return ((size_t)FFTShape<N>::SMEM + RaTw<N>::kEntries + N) * sizeof(float2); }
@@ -1028,6 +1213,11 @@ static cudaError_t set_attrs()
         return e;
     if ((e = cudaFuncSetAttribute(k_ra_pair<N, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, big))) return e;
     if ((e = cudaFuncSetAttribute(k_ra_corr<N>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)corr_smem<N>())))
+        return e;
+    const int sp0 = (int)spec0_smem<N>();
+    if ((e = cudaFuncSetAttribute(k_ra_spec0<N, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, sp0))) return e;
+    if ((e = cudaFuncSetAttribute(k_ra_spec0<N, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, sp0))) return e;
+    if ((e = cudaFuncSetAttribute(k_ra_spec<N>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)corr_smem<N>())))
         return e;
     const int r = (int)ra_fft_smem<N>();
     if ((e = cudaFuncSetAttribute(k_ra_accum<N>, cudaFuncAttributeMaxDynamicSharedMemorySize, r))) return e;
@@ -1053,12 +1243,35 @@ static cudaError_t ra_run_n(const RAArgs& a, cudaStream_t st)
     while ((1 << L) < M) ++L;
     k_zero_shift<<<(M + 255) / 256, 256, 0, st>>>(a.S, a.SQ, M);
     ISAR_COUNT(1);
+    // spectral envelope merge: merged group spectra ping-pong between env_a
+    // (M/2 x N complex) and part (M/4 x N complex)
+    const bool spectral = !a.rows_each_level && L >= 1;
+    if (spectral) {
+        float2* wb[2] = {reinterpret_cast<float2*>(a.env_a), reinterpret_cast<float2*>(a.part)};
+        float2* w0 = L > 1 ? wb[0] : nullptr;
+        if (a.x_iq16)
+            k_ra_spec0<N, true><<<M / 2, T, spec0_smem<N>(), st>>>(a.x, a.y, a.win, a.hq, a.S, a.SQ, w0, a.shifts,
+                                                                   a.given_shifts, a.tw);
+        else
+            k_ra_spec0<N, false><<<M / 2, T, spec0_smem<N>(), st>>>(a.x, a.y, a.win, a.hq, a.S, a.SQ, w0, a.shifts,
+                                                                    a.given_shifts, a.tw);
+        ISAR_COUNT(1);
+        int off = M / 2;
+        for (int lv = 1; lv < L; ++lv) {
+            const int pairs = M >> (lv + 1);
+            k_ra_spec<N><<<pairs, T, corr_smem<N>(), st>>>(wb[(lv - 1) & 1], lv == L - 1 ? nullptr : wb[lv & 1], a.S,
+                                                          a.SQ, lv, a.shifts + off, a.given_shifts, a.tw);
+            ISAR_COUNT(1);
+            off += pairs;
+        }
+        if ((e = cudaGetLastError())) return e;
+    }
     const float* left = nullptr;
     int lstride = 1;
     float* bufs[2] = {a.env_a, a.env_b};
     int cur = 0;
     int shift_off = 0;
-    for (int lv = 0; lv < L; ++lv) {
+    for (int lv = 0; lv < L && !spectral; ++lv) {
         const int s = 1 << lv;
         const int pairs = M / (2 * s);
         const bool last = (lv == L - 1);

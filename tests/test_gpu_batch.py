@@ -52,7 +52,7 @@ def test_batch_equals_single_frame_and_oracle(torch_cuda, gb300):
         t = tunings[(f["M"], f["N"])]
         assert t.af_cluster > 0
         with gb300.Context(f["rp"], stream=torch.cuda.current_stream().cuda_stream) as ctx:
-            ctx.set_tuning(**{k: getattr(t, k) for k in ("ra_pair_min", "ra_rows_per_cta", "ra_rows_final",
+            ctx.set_tuning(**{k: getattr(t, k) for k in ("ra_rows_each_level", "ra_pair_min", "ra_rows_per_cta", "ra_rows_final",
                                                          "af_cluster", "af_tol", "af_iters")})
             single = ctx.image_host(f["e"], f["v"], f["flags"])
         assert rel_l2(img, single) <= 1e-6, (f["M"], f["N"])

@@ -64,10 +64,13 @@ def test_hpc_stage(torch_cuda, gb300):
 
 
 # (256, 8192): the 8192-point paths (warp-level transform of the accumulate
-# kernel from level 1 on, the pair kernel at level 0, the final transform)
+# kernel from level 1 on, the pair kernel at level 0, the final transform).
+# rows_each_level 0: spectral envelope merge; 1: carried envelopes, shifted
+# rows transformed again at every level.
+@pytest.mark.parametrize("rows_each_level", [0, 1])
 @pytest.mark.parametrize("M,N,hpc", [(128, 512, False), (256, 1024, True), (256, 4096, False), (512, 2048, True),
                                      (256, 8192, True)])
-def test_range_align_stage(torch_cuda, gb300, M, N, hpc):
+def test_range_align_stage(torch_cuda, gb300, M, N, hpc, rows_each_level):
     torch = torch_cuda
     e, v = make_frame(M, N, seed=M + N, full=hpc)
     rp = oracle.radar(M, N)
@@ -75,6 +78,7 @@ def test_range_align_stage(torch_cuda, gb300, M, N, hpc):
     y_want, sh_want = oracle.range_align(x, rp)
     flags = gb300.FLAG_HPC if hpc else 0
     with ctx_for(gb300, torch, M, N) as ctx:
+        ctx.set_tuning(ra_rows_each_level=rows_each_level)
         d = to_dev(torch, e)
         dv = torch.from_numpy(v).cuda()
         ctx.stage_range_align(d, dv, flags)
