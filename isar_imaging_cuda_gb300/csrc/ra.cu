@@ -643,21 +643,32 @@ __device__ __forceinline__ float2 spec_half(float2 z, float2 zm, float2 h)
 // / N and stores it into xw (x may equal xw), computes both rows' half-cell
 // powers, correlates the pair, adds the shift to S of row 2j+1 and, when
 // wout is set, stores the merged spectrum W_2j + ramp(s) W_2j+1 as wout[j].
-// IQ16: x holds int16 I/Q pairs.
+// IQ16: x holds int16 I/Q pairs.  Both rows are copied into the CTA's row
+// buffers by bulk asynchronous copies at the start (bounded waits set *err).
 template <int N, bool IQ16>
 __global__ void __launch_bounds__(N / 16)
 k_ra_spec0(const float2* x, float2* xw, const float* __restrict__ win, const int64_t* __restrict__ hq,
            double* __restrict__ S, int64_t* __restrict__ SQ, float2* __restrict__ wout, float* shift_out, int given,
-           const float2* __restrict__ tw)
+           const float2* __restrict__ tw, unsigned* err)
 {
     using F = FFTShape<N>;
     constexpr int D = N / 16;
+    constexpr uint32_t kRowBytes = IQ16 ? N * 2 * sizeof(int16_t) : N * sizeof(float2);
     extern __shared__ float4 dyn_smem[];
+    __shared__ __align__(8) uint64_t bars[2];
     float2* sm = reinterpret_cast<float2*>(dyn_smem);
-    float2* ca = sm + F::SMEM;   // row 2j: (w[2n], w[2n+1]), then its FFT
+    float2* ca = sm + F::SMEM;   // row 2j: x, then (w[2n], w[2n+1]), then its FFT
     float2* cb = ca + N;         // row 2j+1
     float2* twt = cb + N;
     const int lt = threadIdx.x, j = blockIdx.x;
+    RowStage sa{ca, &bars[0], err, 0u}, sb{cb, &bars[1], err, 0u};
+    if (lt == 0) {
+        const char* src = reinterpret_cast<const char*>(x);
+        sa.init();
+        sb.init();
+        sa.issue(src + (size_t)(2 * j) * kRowBytes, kRowBytes);
+        sb.issue(src + (size_t)(2 * j + 1) * kRowBytes, kRowBytes);
+    }
     RaTw<N>::fill(twt, tw, lt, F::T);
     __syncthreads();
     const RaTw<N> tws{twt};
@@ -669,16 +680,18 @@ k_ra_spec0(const float2* x, float2* xw, const float* __restrict__ win, const int
         float2* ur = xw + (size_t)row * N;
         RowPhase<N> rp;
         rp.init(hq ? hq[row] : 0, 0, lt);
-        // even samples: p = IFFT(u); each thread reads, then overwrites, its
-        // own elements of x (in place when x == xw)
+        if (t == 0) sa.wait();
+        else sb.wait();
+        // even samples: p = IFFT(u) from the staged row; u is stored to xw
+        // (the staged copy makes x == xw safe)
         team_fft<N, true>(
             [&](int i) {
                 float2 xv;
                 if constexpr (IQ16) {
-                    const short2 q = reinterpret_cast<const short2*>(x)[(size_t)row * N + i];
+                    const short2 q = reinterpret_cast<const short2*>(c)[i];
                     xv = make_float2((float)q.x, (float)q.y);
                 } else {
-                    xv = x[(size_t)row * N + i];
+                    xv = c[i];
                 }
                 const float2 u = cscale(cmul(xv, rp.at((i - lt) / D)), __ldg(&win[i]) * invN);
                 ur[i] = u;
@@ -703,8 +716,11 @@ k_ra_spec0(const float2* x, float2* xw, const float* __restrict__ win, const int
     if (wout == nullptr) return;
     // Z = FFT(w_even + j w_odd) in place (team_fft reads all its inputs
     // before its first barrier and writes its outputs after the last)
-    team_fft<N, false>([&](int i) { return ca[i]; }, [&](int k, float2 v, int) { ca[k] = v; }, sm, lt, tws);
-    team_fft<N, false>([&](int i) { return cb[i]; }, [&](int k, float2 v, int) { cb[k] = v; }, sm, lt, tws);
+#pragma unroll 1
+    for (int t = 0; t < 2; ++t) {
+        float2* c = t ? cb : ca;
+        team_fft<N, false>([&](int i) { return c[i]; }, [&](int k, float2 v, int) { c[k] = v; }, sm, lt, tws);
+    }
     __syncthreads();
     LinPhase<N> h, r;
     h.init(kHalfCellDown<N>, lt);
@@ -1251,10 +1267,10 @@ static cudaError_t ra_run_n(const RAArgs& a, cudaStream_t st)
         float2* w0 = L > 1 ? wb[0] : nullptr;
         if (a.x_iq16)
             k_ra_spec0<N, true><<<M / 2, T, spec0_smem<N>(), st>>>(a.x, a.y, a.win, a.hq, a.S, a.SQ, w0, a.shifts,
-                                                                   a.given_shifts, a.tw);
+                                                                   a.given_shifts, a.tw, a.err);
         else
             k_ra_spec0<N, false><<<M / 2, T, spec0_smem<N>(), st>>>(a.x, a.y, a.win, a.hq, a.S, a.SQ, w0, a.shifts,
-                                                                    a.given_shifts, a.tw);
+                                                                    a.given_shifts, a.tw, a.err);
         ISAR_COUNT(1);
         int off = M / 2;
         for (int lv = 1; lv < L; ++lv) {
