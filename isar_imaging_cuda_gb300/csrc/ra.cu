@@ -657,7 +657,7 @@ k_ra_spec0(const float2* x, float2* xw, const float* __restrict__ win, const int
     extern __shared__ float4 dyn_smem[];
     __shared__ __align__(8) uint64_t bars[2];
     float2* sm = reinterpret_cast<float2*>(dyn_smem);
-    float2* ca = sm + F::SMEM;   // row 2j: x, then (w[2n], w[2n+1]), then its FFT
+    float2* ca = sm + F::SMEM;   // row 2j: x, then (sqrt w[2n], w[2n+1]), then FFT(w_even + j w_odd)
     float2* cb = ca + N;         // row 2j+1
     float2* twt = cb + N;
     const int lt = threadIdx.x, j = blockIdx.x;
@@ -673,19 +673,28 @@ k_ra_spec0(const float2* x, float2* xw, const float* __restrict__ win, const int
     __syncthreads();
     const RaTw<N> tws{twt};
     const float invN = 1.0f / (float)N;
+    // Four row transforms, k = 2t + odd (one instantiation): t selects the
+    // row, odd = 0 the samples p(n) = IFFT(u), u formed from the staged row
+    // and stored to xw (the staged copy makes x == xw safe), odd = 1 the
+    // samples p(n + 1/2) = IFFT(u * exp(j pi k / N)), u read back by the
+    // thread that stored it.  c[n] = (|p(n)|, |p(n + 1/2)|^2): the amplitude
+    // feeds the correlation, its square the spectrum.
 #pragma unroll 1
-    for (int t = 0; t < 2; ++t) {
+    for (int k = 0; k < 4; ++k) {
+        const int t = k >> 1, odd = k & 1;
         const int row = 2 * j + t;
         float2* c = t ? cb : ca;
+        float* cf = reinterpret_cast<float*>(c) + odd;
         float2* ur = xw + (size_t)row * N;
-        RowPhase<N> rp;
-        rp.init(hq ? hq[row] : 0, 0, lt);
-        if (t == 0) sa.wait();
-        else sb.wait();
-        // even samples: p = IFFT(u) from the staged row; u is stored to xw
-        // (the staged copy makes x == xw safe)
+        RowPhase<N> rp;   // the chirp (even) or the half-cell ramp (odd, no chirp)
+        if (odd) rp.init(0, kHalfCellUp<N>, lt);
+        else rp.init(hq ? hq[row] : 0, 0, lt);
+        if (k == 0) sa.wait();
+        else if (k == 2) sb.wait();
         team_fft<N, true>(
             [&](int i) {
+                const float2 ph = rp.at((i - lt) / D);
+                if (odd) return cmul(ur[i], ph);
                 float2 xv;
                 if constexpr (IQ16) {
                     const short2 q = reinterpret_cast<const short2*>(c)[i];
@@ -693,20 +702,18 @@ k_ra_spec0(const float2* x, float2* xw, const float* __restrict__ win, const int
                 } else {
                     xv = c[i];
                 }
-                const float2 u = cscale(cmul(xv, rp.at((i - lt) / D)), __ldg(&win[i]) * invN);
+                const float2 u = cscale(cmul(xv, ph), __ldg(&win[i]) * invN);
                 ur[i] = u;
                 return u;
             },
-            [&](int n, float2 v, int) { c[n].x = v.x * v.x + v.y * v.y; }, sm, lt, tws);
-        // odd samples: p(n + 1/2) = IFFT(u * exp(j pi k / N)); the thread
-        // reads back the u it stored itself
-        LinPhase<N> hp;
-        hp.init(kHalfCellUp<N>, lt);
-        team_fft<N, true>([&](int i) { return cmul(ur[i], hp.at((i - lt) / D)); },
-                          [&](int n, float2 v, int) { c[n].y = v.x * v.x + v.y * v.y; }, sm, lt, tws);
+            [&](int n, float2 v, int) {
+                const float w = v.x * v.x + v.y * v.y;
+                cf[2 * n] = odd ? w : sqrtf(w);
+            },
+            sm, lt, tws);
     }
     __syncthreads();
-    const float shc = ra_correlate_f<N>([&](int n) { return sqrtf(ca[n].x); }, [&](int n) { return sqrtf(cb[n].x); },
+    const float shc = ra_correlate_f<N>([&](int n) { return ca[n].x; }, [&](int n) { return cb[n].x; },
                                         reinterpret_cast<float*>(sm), lt, tws);
     const float sh = given ? shift_out[j] : shc;   // given: shifts injected by the caller (test hook)
     if (lt == 0) {
@@ -719,7 +726,12 @@ k_ra_spec0(const float2* x, float2* xw, const float* __restrict__ win, const int
 #pragma unroll 1
     for (int t = 0; t < 2; ++t) {
         float2* c = t ? cb : ca;
-        team_fft<N, false>([&](int i) { return c[i]; }, [&](int k, float2 v, int) { c[k] = v; }, sm, lt, tws);
+        team_fft<N, false>(
+            [&](int i) {
+                const float2 v = c[i];
+                return make_float2(v.x * v.x, v.y);
+            },
+            [&](int k, float2 v, int) { c[k] = v; }, sm, lt, tws);
     }
     __syncthreads();
     LinPhase<N> h, r;
