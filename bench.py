@@ -131,12 +131,18 @@ def peaks():
 
 
 def ra_algorithmic_bytes(M, N):
-    """Compulsory HBM bytes of range alignment as this project formulates it:
-    level 0 reads all M rows (8MN) and stores the first-half envelopes (2MN);
-    levels 1..L-1 read the M/2 shifted rows (4MN each); the final transform
-    reads and writes every row (16MN)."""
+    """Compulsory HBM bytes of range alignment as this project formulates it
+    (spectral envelope merge): level 0 reads all M rows (8MN) and stores the
+    M/2 merged group spectra (N complex each, 4MN); level l >= 1 reads its
+    M/2^l group spectra and, below the last level, stores M/2^(l+1) merged
+    ones; the final transform reads and writes every row (16MN)."""
     L = M.bit_length() - 1
-    return 8 * M * N + 2 * M * N + (L - 1) * 4 * M * N + 16 * M * N
+    b = 8 * M * N + (4 * M * N if L > 1 else 0) + 16 * M * N
+    for lv in range(1, L):
+        b += (M >> lv) * N * 8
+        if lv < L - 1:
+            b += (M >> (lv + 1)) * N * 8
+    return b
 
 
 def image_entropy(img):
@@ -326,8 +332,8 @@ def run_gb300(args):
 
     peak, peak_kind = peaks()
     ra_bytes = ra_algorithmic_bytes(M, N)
-    roof = {"kernel": "range alignment, 1024 x 8192 (k_ra_pair/k_ra_accum/k_ra_corr levels + k_ra_final, "
-                      "HPC fused), single frame", "bound": "hbm",
+    roof = {"kernel": "range alignment, 1024 x 8192 (k_ra_spec0 + k_ra_spec levels + k_ra_final, spectral "
+                      "envelope merge, HPC fused), single frame", "bound": "hbm",
             "achieved": ra_bytes / (stage_ms["range_align"] * 1e-3) / 1e9, "algorithmic_bytes": ra_bytes,
             "ms": stage_ms["range_align"], "peak": peak, "unit": "GB/s", "peak_kind": peak_kind,
             "traffic": RA_STAGE_TRAFFIC}

@@ -9,11 +9,19 @@
 // by a linear phase ramp.  Here x is never rewritten: every row carries a
 // cumulative shift S_m (cells) and a high-speed-compensation coefficient, and
 // each load applies window * exp(j*2*pi*(alpha_m*n^2 - S_m*n/N)) on the fly
-// (64-bit fixed-point phase, exact modulo one cycle).  Rows of the first half
-// of a group are unchanged since the previous level, so their envelope is
-// carried over ("left" vector) and only the rows shifted by the previous
-// level are transformed again: (log2 M - 1) * M/2 + 2M row FFTs instead of
-// (log2 M + 1) * M.
+// (64-bit fixed-point phase, exact modulo one cycle).  Two ways to form the
+// group envelopes (isar_tuning.ra_rows_each_level):
+//  - spectral merge (default): every group carries the 2N-point spectrum of
+//    its half-cell power envelope, which a shift multiplies by a phase ramp
+//    and a merge adds (k_ra_spec0, k_ra_spec): 4M + 3 (M/2 - 1) + M
+//    transforms of N points per frame;
+//  - carried envelopes: rows of the first half of a group are unchanged
+//    since the previous level, so their envelope is carried over ("left"
+//    vector) and only the rows shifted by the previous level are transformed
+//    again (k_ra_pair, k_ra_accum, k_ra_corr): (log2 M - 1) * M/2 + 2M row
+//    transforms plus 2 (M - 1) correlation transforms.
+// The reference transforms all rows at every level: (log2 M + 1) * M row
+// transforms plus 3 (M - 1) correlation transforms.
 #include <cuda_runtime.h>
 
 #include <type_traits>
