@@ -47,9 +47,10 @@ ARMS = [("learned warm start + entropy stop criterion", True, TOL),
 WORKLOAD = ("full five-stage pipeline, 1024 pulses x 8192 range cells complex64, HPC + MTRC on, "
             "batches of 32 frames")
 # DRAM bytes (read + write) of one range-alignment stage at 1024 x 8192, all
-# its kernels, per frame: dram__bytes_read.sum + dram__bytes_write.sum from
-# an ncu capture of `bench.py --profile plain` (two frames, halved)
-RA_STAGE_TRAFFIC = 547067648
+# its kernels, per frame (spectral envelope merge): dram__bytes_read.sum +
+# dram__bytes_write.sum from an ncu capture of `bench.py --profile plain`
+# (two frames, halved); writes still in L2 at a kernel's end are not counted
+RA_STAGE_TRAFFIC = 251913088
 
 
 def dist_init():
