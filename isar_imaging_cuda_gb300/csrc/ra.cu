@@ -665,9 +665,16 @@ k_ra_spec0(const float2* x, float2* xw, const float* __restrict__ win, const int
     extern __shared__ float4 dyn_smem[];
     __shared__ __align__(8) uint64_t bars[2];
     float2* sm = reinterpret_cast<float2*>(dyn_smem);
+    // Row buffers: the staged row (contiguous), then c[n] at pc(n).  At
+    // N = 8192 the row transforms run on fft8192, whose outputs arrive 16
+    // apart across lanes: one pad slot per 16 keeps those stores apart in
+    // the shared-memory banks.
+    constexpr bool kWarp = (N == 8192);
+    constexpr int CS = kWarp ? N + N / 16 : N;
+    auto pc = [](int i) { return kWarp ? i + (i >> 4) : i; };
     float2* ca = sm + F::SMEM;   // row 2j: x, then (sqrt w[2n], w[2n+1]), then FFT(w_even + j w_odd)
-    float2* cb = ca + N;         // row 2j+1
-    float2* twt = cb + N;
+    float2* cb = ca + CS;        // row 2j+1
+    float2* twt = cb + CS;
     const int lt = threadIdx.x, j = blockIdx.x;
     RowStage sa{ca, &bars[0], err, 0u}, sb{cb, &bars[1], err, 0u};
     if (lt == 0) {
@@ -699,7 +706,7 @@ k_ra_spec0(const float2* x, float2* xw, const float* __restrict__ win, const int
         else rp.init(hq ? hq[row] : 0, 0, lt);
         if (k == 0) sa.wait();
         else if (k == 2) sb.wait();
-        team_fft<N, true>(
+        row_fft<N, true, kWarp>(
             [&](int i) {
                 const float2 ph = rp.at((i - lt) / D);
                 if (odd) return cmul(ur[i], ph);
@@ -716,12 +723,12 @@ k_ra_spec0(const float2* x, float2* xw, const float* __restrict__ win, const int
             },
             [&](int n, float2 v, int) {
                 const float w = v.x * v.x + v.y * v.y;
-                cf[2 * n] = odd ? w : sqrtf(w);
+                cf[2 * pc(n)] = odd ? w : sqrtf(w);
             },
-            sm, lt, tws);
+            sm, lt, tws, NoHook{});
     }
     __syncthreads();
-    const float shc = ra_correlate_f<N>([&](int n) { return ca[n].x; }, [&](int n) { return cb[n].x; },
+    const float shc = ra_correlate_f<N>([&](int n) { return ca[pc(n)].x; }, [&](int n) { return cb[pc(n)].x; },
                                         reinterpret_cast<float*>(sm), lt, tws);
     const float sh = given ? shift_out[j] : shc;   // given: shifts injected by the caller (test hook)
     if (lt == 0) {
@@ -736,10 +743,10 @@ k_ra_spec0(const float2* x, float2* xw, const float* __restrict__ win, const int
         float2* c = t ? cb : ca;
         team_fft<N, false>(
             [&](int i) {
-                const float2 v = c[i];
+                const float2 v = c[pc(i)];
                 return make_float2(v.x * v.x, v.y);
             },
-            [&](int k, float2 v, int) { c[k] = v; }, sm, lt, tws);
+            [&](int k, float2 v, int) { c[pc(k)] = v; }, sm, lt, tws);
     }
     __syncthreads();
     LinPhase<N> h, r;
@@ -751,8 +758,8 @@ k_ra_spec0(const float2* x, float2* xw, const float* __restrict__ win, const int
         const int d = lt + q * D;
         const int dm = (N - d) & (N - 1);
         const float2 hd = h.at(q), rd = r.at(q);
-        const float2 wa = spec_half(ca[d], ca[dm], hd);
-        const float2 wb = cmul(rd, spec_half(cb[d], cb[dm], hd));
+        const float2 wa = spec_half(ca[pc(d)], ca[pc(dm)], hd);
+        const float2 wb = cmul(rd, spec_half(cb[pc(d)], cb[pc(dm)], hd));
         w[d] = make_float2(wa.x + wb.x, wa.y + wb.y);
     }
 }
@@ -1229,7 +1236,11 @@ template <int N>
 static size_t pair_smem() { return corr_smem<N>() + N * sizeof(float2); }
 // spectral level 0: FFT scratch + two rows of half-cell powers + twiddle table
 template <int N>
-static size_t spec0_smem() { return ((size_t)FFTShape<N>::SMEM + 2 * N + RaTw<N>::kEntries) * sizeof(float2); }
+static size_t spec0_smem()
+{
+    constexpr size_t CS = (N == 8192) ? N + N / 16 : N;
+    return ((size_t)FFTShape<N>::SMEM + 2 * CS + RaTw<N>::kEntries) * sizeof(float2);
+}
 // range-alignment row kernels: FFT scratch + twiddle table + row staging buffer
 template <int N>
 static size_t ra_fft_smem() { return ((size_t)FFTShape<N>::SMEM + RaTw<N>::kEntries + N) * sizeof(float2); }
