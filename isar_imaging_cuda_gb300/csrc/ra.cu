@@ -736,17 +736,18 @@ k_ra_spec0(const float2* x, float2* xw, const float* __restrict__ win, const int
         add_shift(S, SQ, (size_t)2 * j + 1, sh, N);
     }
     if (wout == nullptr) return;
-    // Z = FFT(w_even + j w_odd) in place (team_fft reads all its inputs
-    // before its first barrier and writes its outputs after the last)
+    // Z = FFT(w_even + j w_odd) in place (both transforms read all their
+    // inputs before their first barrier and write their outputs after the
+    // last)
 #pragma unroll 1
     for (int t = 0; t < 2; ++t) {
         float2* c = t ? cb : ca;
-        team_fft<N, false>(
+        row_fft<N, false, kWarp>(
             [&](int i) {
                 const float2 v = c[pc(i)];
                 return make_float2(v.x * v.x, v.y);
             },
-            [&](int k, float2 v, int) { c[pc(k)] = v; }, sm, lt, tws);
+            [&](int k, float2 v, int) { c[pc(k)] = v; }, sm, lt, tws, NoHook{});
     }
     __syncthreads();
     LinPhase<N> h, r;
