@@ -630,8 +630,9 @@ k_ra_corr(const float* __restrict__ E, double* __restrict__ S, int64_t* __restri
 // every shifted row of the group again.  w is real, so W is Hermitian and
 // only d in [0, N) is kept; W[N] is zero (p has no lag of N).
 
-// exp(-j 2 pi sq n / 2^64) slopes for LinPhase: exp(+j pi n / N) (the odd
-// samples p(n + 1/2)) and exp(-j pi n / N) (the odd half of W).
+// Linear phase slopes sq of exp(-j 2 pi sq n / 2^64) (LinPhase, RowPhase
+// without chirp): exp(+j pi n / N) (the odd samples p(n + 1/2)) and
+// exp(-j pi n / N) (the odd half of W).
 template <int N>
 constexpr int64_t kHalfCellUp = (int64_t)(0ull - ((1ull << 63) / (uint64_t)N));
 template <int N>
