@@ -18,8 +18,9 @@ algorithm: cooperative autofocus, 120 iterations), timed the same way.
 `e2e` goes through the public C ABI with pinned host buffers: every step
 copies its 32 echoes host->device as int16 I/Q samples (the sensor format, 4
 bytes per sample; range alignment reads them directly) and reads the 32
-images back, double buffered against the previous step's compute.  Under torchrun every rank
-images its own frames (replicas, weak scaling).
+images back, three buffer sets in rotation so that the copies of the next steps overlap the
+current step's compute.  Under torchrun every rank images its own frames (replicas, weak
+scaling).
 
 --impl reference times the CPU restatement of the reference's chain (the
 oracle) on all host cores, one frame per worker process per step.
@@ -40,6 +41,7 @@ M, N = 1024, 8192
 C = 512
 B = 32                      # frames per batch step
 TOL = 3e-7                  # autofocus entropy stop criterion (relative change per iteration)
+E2E_SETS = 3                # end-to-end buffer sets in rotation (copies of later steps run ahead)
 METRIC = "frames/s @1024×8192 c64: learned+batched vs plain on 1 GB300, equal entropy"
 ARMS = [("learned warm start + entropy stop criterion", True, TOL),
         ("entropy stop criterion, Doppler-tracking start", False, TOL),
@@ -280,45 +282,46 @@ def run_gb300(args):
     ms = max_over_ranks(ws, ms, dev)
     barrier(ws)
 
-    # ---- end to end: pinned host echoes in, images out, double buffered ----
+    # ---- end to end: pinned host echoes in, images out, E2E_SETS buffer sets ----
     # The echoes travel as the sensor's int16 I/Q samples (the frames are
     # int16-quantised: the same samples) and range alignment reads them
     # directly (ISAR_FLAG_IQ16).
     HQ = torch.empty((B, M, 2 * N), dtype=torch.int16, pin_memory=True)
     HQ.copy_(X.to(torch.int16).cpu())
     HV = V.cpu().pin_memory()
-    Q = [torch.empty((B, M, 2 * N), dtype=torch.int16, device=dev) for _ in range(2)]
+    Q = [torch.empty((B, M, 2 * N), dtype=torch.int16, device=dev) for _ in range(E2E_SETS)]
     fq = flags | g.FLAG_IQ16
-    HI = [torch.empty((B, M, C), dtype=torch.float32, pin_memory=True) for _ in range(2)]
-    V2 = torch.empty_like(V)
-    imgs2 = torch.empty_like(imgs)
-    sets = [(Q[0], V, imgs, g.Batch.frames((rp, Q[0][i], V[i], fq, imgs[i]) for i in range(B))),
-            (Q[1], V2, imgs2, g.Batch.frames((rp, Q[1][i], V2[i], fq, imgs2[i]) for i in range(B)))]
+    HI = [torch.empty((B, M, C), dtype=torch.float32, pin_memory=True) for _ in range(E2E_SETS)]
+    Vs = [V] + [torch.empty_like(V) for _ in range(E2E_SETS - 1)]
+    Is = [imgs] + [torch.empty_like(imgs) for _ in range(E2E_SETS - 1)]
+    sets = [(Q[k], Vs[k], Is[k], g.Batch.frames((rp, Q[k][i], Vs[k][i], fq, Is[k][i]) for i in range(B)))
+            for k in range(E2E_SETS)]
     # three streams: host->device copies (cs), the batch (s), device->host
-    # copies (ds); buffer set i % 2 is reused two steps later
+    # copies (ds); buffer set i % E2E_SETS is reused E2E_SETS steps later
     cs = torch.cuda.Stream(device=dev)
     ds = torch.cuda.Stream(device=dev)
-    h2d_done = [torch.cuda.Event() for _ in range(2)]
-    run_done = [torch.cuda.Event() for _ in range(2)]
-    d2h_done = [torch.cuda.Event() for _ in range(2)]
+    h2d_done = [torch.cuda.Event() for _ in range(E2E_SETS)]
+    run_done = [torch.cuda.Event() for _ in range(E2E_SETS)]
+    d2h_done = [torch.cuda.Event() for _ in range(E2E_SETS)]
     for e in run_done + d2h_done:
         e.record(s)
 
     def e2e_step(i):
-        Qd, Vd, Id, L = sets[i % 2]
-        cs.wait_event(run_done[i % 2])       # step i-2 has consumed Qd, Vd
+        k = i % E2E_SETS
+        Qd, Vd, Id, L = sets[k]
+        cs.wait_event(run_done[k])           # the set's previous batch has consumed Qd, Vd
         with torch.cuda.stream(cs):
             Qd.copy_(HQ, non_blocking=True)
             Vd.copy_(HV, non_blocking=True)
-            h2d_done[i % 2].record(cs)
-        s.wait_event(h2d_done[i % 2])
-        s.wait_event(d2h_done[i % 2])        # step i-2's images are read back
+            h2d_done[k].record(cs)
+        s.wait_event(h2d_done[k])
+        s.wait_event(d2h_done[k])            # the set's previous images are read back
         batch.run(L)
-        run_done[i % 2].record(s)
-        ds.wait_event(run_done[i % 2])
+        run_done[k].record(s)
+        ds.wait_event(run_done[k])
         with torch.cuda.stream(ds):
-            HI[i % 2].copy_(Id, non_blocking=True)
-            d2h_done[i % 2].record(ds)
+            HI[k].copy_(Id, non_blocking=True)
+            d2h_done[k].record(ds)
 
     for i in range(args.warmup):
         e2e_step(i)
@@ -373,7 +376,7 @@ def run_gb300(args):
     if rank == 0 and not args.no_cpu:
         out["cpu_baseline"] = cpu_baseline(X[0], V[0])
     if rank == 0:
-        del X, V2, imgs, imgs2, HQ, Q
+        del X, Vs, Is, imgs, HQ, Q, sets
         torch.cuda.empty_cache()
         out["other_workloads"] = other_workloads(g, torch, s, args.steps)
     if rank == 0:
