@@ -247,7 +247,9 @@ ISAR_API int isar_center_cut_noalloc(const float* d_profiles, int echo_num, int 
 
 /*
  * Autotuner (no counterpart in the reference): times whole frames of
- * d_echo on this context over the range-alignment knobs and the autofocus
+ * d_echo on this context over the range-alignment knobs (envelope path, then
+ * the carried-envelope path's pair threshold and rows per CTA when that path
+ * wins, then the final transform's rows per CTA) and the autofocus
  * engines allowed by `engines` (bit 0: cooperative grid, bit 1: clusters),
  * coordinate by coordinate, applies the fastest and returns it.  Keeps
  * af_tol and af_iters.  Blocking; allocates a scratch image while it runs.
@@ -288,7 +290,8 @@ ISAR_API int isar_batch_lanes(isar_batch* b);
 ISAR_API int isar_batch_set_warmstart(isar_batch* b, const isar_wsnet* net);
 /* Tunes each shape (isar_autotune, cluster engine), then on the whole frame
  * list the lanes per shape with the cluster size, then the range-alignment
- * rows per CTA; *best_ms (may be NULL) = the fastest batch time. */
+ * envelope path and rows per CTA; *best_ms (may be NULL) = the fastest batch
+ * time. */
 ISAR_API int isar_batch_autotune(isar_batch* b, const isar_batch_frame* frames, int n, float* best_ms);
 
 /* ---- learned autofocus warm start ----------------------------------------
