@@ -92,3 +92,68 @@ def test_binary_merge_envelopes_match_direct_sums():
     Wg, rows = groups[0]
     direct = sum(np.abs(np.fft.ifft(shifted(U[m], S[m])) * N) ** 2 for m in rows)
     assert np.allclose(envelope(Wg), direct, rtol=0, atol=1e-9 * direct.max())
+
+
+def _f32_window(N):
+    """hamming(n) * cos(pi n) in float as the reference forms it (the oracle's
+    window up to the last rounding of cos)."""
+    n = np.arange(N)
+    f32 = np.float32
+    ham = (f32(0.54) - f32(0.46) * np.cos((f32(2 * np.pi) * n.astype(f32)) / f32(N - 1)).astype(f32)).astype(f32)
+    return (ham * np.cos((f32(np.pi) * n.astype(f32)).astype(np.float64)).astype(f32)).astype(f32)
+
+
+def _f32_shift(a, b):
+    """The pair shift as the range-alignment kernels compute it: complex64
+    transforms locate the peak, the three parabola samples are exact sums,
+    the parabola is fitted in float."""
+    sf = pytest.importorskip("scipy.fft")
+    f32 = np.float32
+    N = a.shape[0]
+    c = sf.ifft(sf.fft(a.astype(np.complex64)) * np.conj(sf.fft(b.astype(np.complex64)))).real
+    pos = int(np.argmax(np.abs(np.roll(c, N // 2))))
+    tau = (pos + N // 2) % N
+    f = [f32(np.dot(a.astype(np.float64), np.roll(b.astype(np.float64), tau + j - 1))) for j in range(3)]
+    fa = (f[0] + f[2] - f32(2) * f[1]) / f32(2)
+    fb = (f[2] - f[0]) / f32(2)
+    return f32(f32(pos) + (-fb / (f32(2) * fa))) - f32(N / 2)
+
+
+@pytest.mark.parametrize("M,N,full", [(128, 512, False), (256, 1024, True)])
+def test_fp32_spectral_formulation_reproduces_the_oracle_shifts(M, N, full):
+    """The spectral merge in complex64 arithmetic (the kernels' precision)
+    gives the FP64 oracle's range-alignment shifts on seeded frames."""
+    sf = pytest.importorskip("scipy.fft")
+    import oracle
+    from tests.helpers import make_frame
+    e, v = make_frame(M, N, seed=M + N, full=full)
+    rp = oracle.radar(M, N)
+    x = oracle.hpc(e, v, rp) if full else e.astype(np.complex128)
+    _, want = oracle.range_align(x, rp)
+    u = (x * _f32_window(N)[None, :] / N).astype(np.complex64)
+    k = np.arange(N)
+    p0 = sf.ifft(u, axis=1) * N
+    p1 = sf.ifft((u * np.exp(1j * np.pi * k / N)).astype(np.complex64), axis=1) * N
+    c = ((np.abs(p0) ** 2) + 1j * (np.abs(p1) ** 2)).astype(np.complex64)
+    Z = sf.fft(c, axis=1)
+    Zm = np.conj(Z[:, (-k) % N])
+    W = ((Z + Zm) / 2 + np.exp(-1j * np.pi * k / N) * (Z - Zm) / 2j).astype(np.complex64)
+    amp = np.abs(p0).astype(np.float32)
+    got, G = [], []
+    for j in range(M // 2):
+        s = _f32_shift(amp[2 * j], amp[2 * j + 1])
+        got.append(s)
+        G.append((W[2 * j] + np.exp(-2j * np.pi * k * float(s) / N) * W[2 * j + 1]).astype(np.complex64))
+    while len(G) > 1:
+        nxt = []
+        for Wa, Wb in zip(G[0::2], G[1::2]):
+            X = [Wg + np.conj(Wg[(N - k) % N]) for Wg in (Wa, Wb)]
+            for Xg, Wg in zip(X, (Wa, Wb)):
+                Xg[0] = Wg[0]
+            env = sf.ifft((X[0] + 1j * X[1]).astype(np.complex64)) * N / (2 * N)
+            s = _f32_shift(np.sqrt(np.maximum(env.real, 0)).astype(np.float32),
+                           np.sqrt(np.maximum(env.imag, 0)).astype(np.float32))
+            got.append(s)
+            nxt.append((Wa + np.exp(-2j * np.pi * k * float(s) / N) * Wb).astype(np.complex64))
+        G = nxt
+    assert np.max(np.abs(np.array(got, np.float64) - want)) < 2e-3
