@@ -1,11 +1,13 @@
-"""The identity behind the range-alignment spectral envelope merge, in FP64
-numpy (no GPU): the 2N-point spectrum of a row's half-cell power
+"""The identity behind the range-alignment spectral envelope merge, in numpy
+(no GPU): the 2N-point spectrum of a row's half-cell power
 w[2n] = |p(n)|^2, w[2n+1] = |p(n + 1/2)|^2 turns a shift of the row by s
 cells (ramp exp(-j 2 pi k s / N) on its spectrum, k = 0..N-1, as the
 reference's rangeAlignmentParallel applies it) into the phase ramp
 exp(-j 2 pi d s / N) on the lag d, so a group's power envelope is the even-
-sample inverse transform of the sum of its rows' shifted spectra.  The CUDA
-kernels k_ra_spec0 / k_ra_spec follow these steps in FP32."""
+sample inverse transform of the sum of its rows' shifted spectra (checked in
+FP64).  The CUDA kernels k_ra_spec0 / k_ra_spec follow these steps in FP32;
+a complex64 run of the whole formulation is checked against the FP64
+oracle's shifts."""
 import numpy as np
 import pytest
 
