@@ -234,8 +234,10 @@ ISAR_API int isar_set_ra_shifts(isar_ctx* ctx, const float* shifts);
  * (a fixed, pre-reserved memory budget; cudaMalloc/cudaFree, which can
  * synchronise the device, are not allowed inside their processing loop).
  *
- * Scratch is one static device array per device, sized for
- * range_num <= 8192; larger range_num returns ISAR_EINVAL.  The first call on
+ * Sizes are those of isar_create: echo_num a power of two in [128, 1024],
+ * range_num a power of two in [512, 8192].  Scratch is one static device
+ * array per device, sized for range_num <= 8192; larger range_num returns
+ * ISAR_EINVAL.  The first call on
  * each device sets up (symbol address and a kernel attribute, no allocation);
  * make that first call before capturing a stream, e.g. with all arguments
  * NULL/0, which performs the set-up only.  Calls that overlap in time on one

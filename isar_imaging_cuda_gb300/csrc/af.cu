@@ -1046,14 +1046,12 @@ struct AfEngine {
     }
 };
 
-// Cluster engine set-up (once per process): shared-memory limit, non-portable
+// Cluster engine set-up (once per device): shared-memory limit, non-portable
 // cluster sizes, and the largest of 16/8/4 CTAs per cluster that can be
 // resident.  Returns that size, 0 if none, or a negative cudaError_t.
 template <int M>
-static int af_cluster_setup()
+static int af_cluster_probe()
 {
-    static int max_cl = -1;
-    if (max_cl >= 0) return max_cl;
     using A = AfEngine<M>;
     cudaError_t e;
     if ((e = cudaFuncSetAttribute(A::kernel(), cudaFuncAttributeMaxDynamicSharedMemorySize, (int)A::SMEM)))
@@ -1078,8 +1076,14 @@ static int af_cluster_setup()
         if (cudaOccupancyMaxActiveClusters(&n, A::kernel(), &cfg) == cudaSuccess && n > 0) best = cl;
         (void)cudaGetLastError();
     }
-    max_cl = best;
-    return max_cl;
+    return best;
+}
+
+template <int M>
+static int af_cluster_setup()
+{
+    static PerDevice max_cl;
+    return max_cl.get(af_cluster_probe<M>);
 }
 
 template <int M>
@@ -1130,22 +1134,25 @@ static cudaError_t fe_run_m(const FEArgs& a, cudaStream_t st)
     const size_t smem = ((size_t)CB * F::SMEM + TwShared<M>::kEntries) * sizeof(float2);
     const size_t smem_p = (size_t)4 * M * sizeof(float2) + (size_t)4 * F::SMEM * sizeof(float2) + M * sizeof(float2) +
                           TwShared<M>::kEntries * sizeof(float2);
-    static int grid_p = 0;
-    if (grid_p == 0) {
+    // per device: shared-memory limits, and whether the cooperative grid of
+    // 128 CTAs (at most 4 of the <= 512 bins each) can be co-resident
+    static PerDevice setup;
+    const int su = setup.get([smem, smem_p]() -> int {
         cudaError_t e;
         if ((e = cudaFuncSetAttribute(k_fe_colfft<M, CB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)))
-            return e;
+            return -(int)e;
         if ((e = cudaFuncSetAttribute(k_af_persist<M>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_p)))
-            return e;
+            return -(int)e;
         int dev = 0, sms = 0, per_sm = 0;
-        cudaGetDevice(&dev);
-        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        if ((e = cudaGetDevice(&dev))) return -(int)e;
+        if ((e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev))) return -(int)e;
         if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_af_persist<M>, 4 * F::T, smem_p)))
-            return e;
-        // 128 CTAs own at most 4 of the <= 512 bins each; all must be co-resident
-        grid_p = 128;
-        if (per_sm * sms < grid_p) return cudaErrorCooperativeLaunchTooLarge;
-    }
+            return -(int)e;
+        return per_sm * sms;
+    });
+    if (su < 0) return (cudaError_t)(-su);
+    constexpr int grid_p = 128;
+    if (su < grid_p) return cudaErrorCooperativeLaunchTooLarge;
     const int rows_max = M < 256 ? M : 256;
     const int R = 8;
     const int nparts = (rows_max + R - 1) / R;

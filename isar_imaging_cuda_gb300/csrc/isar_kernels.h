@@ -5,6 +5,7 @@
 #include <stdint.h>
 
 #include <atomic>
+#include <mutex>
 
 namespace isar {
 
@@ -20,6 +21,42 @@ inline std::atomic<long long>& launch_counter()
     return n;
 }
 #define ISAR_COUNT(n) (::isar::launch_counter() += (n))
+
+// One value per device ordinal, computed once per device by a set-up function
+// run with that device current (kernel attributes, occupancy queries: both
+// are per device).  Thread-safe; a negative result (an error) is returned
+// but not kept, so the next call retries.  Devices beyond kSlots are set up
+// on every call.
+class PerDevice {
+  public:
+    PerDevice()
+    {
+        for (auto& v : val_) v.store(kUnset, std::memory_order_relaxed);
+    }
+    template <class F>
+    int get(F&& setup)
+    {
+        int dev = 0;
+        if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kSlots) {
+            (void)cudaGetLastError();
+            return setup();
+        }
+        int v = val_[dev].load(std::memory_order_acquire);
+        if (v != kUnset) return v;
+        std::lock_guard<std::mutex> lock(mu_);
+        v = val_[dev].load(std::memory_order_relaxed);
+        if (v != kUnset) return v;
+        v = setup();
+        if (v >= 0) val_[dev].store(v, std::memory_order_release);
+        return v;
+    }
+
+  private:
+    static constexpr int kSlots = 64;
+    static constexpr int kUnset = -0x7fffffff;
+    std::atomic<int> val_[kSlots];
+    std::mutex mu_;
+};
 
 struct RAArgs {
     int M, N;

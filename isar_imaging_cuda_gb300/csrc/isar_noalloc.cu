@@ -86,8 +86,9 @@ ISAR_API int isar_center_cut_noalloc(const float* d_profiles, int echo_num, int 
         }
         if (range_num < kRangeCut || (range_num & (range_num - 1)) != 0)
             return isar::record_error(ISAR_EINVAL, "range_num must be a power of two in [512, 8192]");
-        if (echo_num < 1 || echo_num > 65535)
-            return isar::record_error(ISAR_EINVAL, "echo_num must be in [1, 65535]");
+        // the pulse counts every other entry point accepts (isar_create)
+        if (echo_num < 128 || echo_num > isar::kMaxM || (echo_num & (echo_num - 1)) != 0)
+            return isar::record_error(ISAR_EINVAL, "echo_num must be a power of two in [128, 1024]");
     }
     float* s = nullptr;
     const int rc = scratch_for_current_device(&s);

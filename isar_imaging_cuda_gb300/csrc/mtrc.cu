@@ -168,18 +168,19 @@ static cudaError_t post_run_m(const PostArgs& a, cudaStream_t st)
     const size_t smem_post = (size_t)CB * F::SMEM * sizeof(float2) + (size_t)M * CB * sizeof(float);
     const size_t smem_cols = (size_t)CB * F::SMEM * sizeof(float2);
     const size_t smem_czt = (size_t)CZ * FL::SMEM * sizeof(float2) + (size_t)M * CZ * sizeof(float2);
-    static bool attr = false;
-    if (!attr) {
+    static PerDevice attr;   // shared-memory limits, set once per device
+    const int ar = attr.get([smem_post, smem_cols, smem_czt]() -> int {
         cudaError_t e;
         if ((e = cudaFuncSetAttribute(k_post<M, CB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_post)))
-            return e;
+            return -(int)e;
         if ((e = cudaFuncSetAttribute(k_mtrc_cols<M, CB>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                       (int)smem_cols)))
-            return e;
+            return -(int)e;
         if ((e = cudaFuncSetAttribute(k_czt<M, CZ>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_czt)))
-            return e;
-        attr = true;
-    }
+            return -(int)e;
+        return 0;
+    });
+    if (ar < 0) return (cudaError_t)(-ar);
     int src_shift = 0;
     const float2* src = a.cut;
     if (a.mtrc) {

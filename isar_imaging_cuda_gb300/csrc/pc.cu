@@ -135,13 +135,12 @@ size_t pc_smem()
 template <int NF>
 cudaError_t pc_launch(const PCArgs& a, cudaStream_t st)
 {
-    static bool attr = false;
-    if (!attr) {
-        cudaError_t e =
-            cudaFuncSetAttribute(k_pulse_compress<NF>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)pc_smem<NF>());
-        if (e) return e;
-        attr = true;
-    }
+    static PerDevice attr;   // shared-memory limit, set once per device
+    const int ar = attr.get([]() -> int {
+        return -(int)cudaFuncSetAttribute(k_pulse_compress<NF>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                          (int)pc_smem<NF>());
+    });
+    if (ar < 0) return (cudaError_t)(-ar);
     k_pulse_compress<NF><<<a.pulses, NF / 16, pc_smem<NF>(), st>>>(a);
     ISAR_COUNT(1);
     return cudaGetLastError();

@@ -1251,10 +1251,8 @@ template <int N>
 static size_t fft_smem() { return (size_t)FFTShape<N>::SMEM * sizeof(float2); }
 
 template <int N>
-static cudaError_t set_attrs()
+static cudaError_t set_attrs_now()
 {
-    static bool done = false;
-    if (done) return cudaSuccess;
     cudaError_t e;
     const int big = (int)pair_smem<N>();
     if ((e = cudaFuncSetAttribute(k_ra_pair<N, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, big))) return e;
@@ -1277,8 +1275,16 @@ static cudaError_t set_attrs()
     if ((e = cudaFuncSetAttribute(k_fft_rows<N, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, f))) return e;
     if ((e = cudaFuncSetAttribute(k_fft_rows<N, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, f))) return e;
     if ((e = cudaFuncSetAttribute(k_hrrp<N>, cudaFuncAttributeMaxDynamicSharedMemorySize, f))) return e;
-    done = true;
     return cudaSuccess;
+}
+
+// Shared-memory limits of the row kernels for N cells, set once per device.
+template <int N>
+static cudaError_t set_attrs()
+{
+    static PerDevice done;
+    const int r = done.get([]() -> int { return -(int)set_attrs_now<N>(); });
+    return r < 0 ? (cudaError_t)(-r) : cudaSuccess;
 }
 
 template <int N>
@@ -1423,13 +1429,9 @@ cudaError_t hpc_apply(float2* x, const int64_t* hq, int M, int N, cudaStream_t s
 
 cudaError_t center_cut(const float* arp, const float2* y, int M, int N, int* dec, float2* cut, cudaStream_t st)
 {
-    static bool attr = false;
-    if (!attr) {
-        cudaError_t e = cudaFuncSetAttribute(k_center, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                             2 * kMaxN * (int)sizeof(float));
-        if (e) return e;
-        attr = true;
-    }
+    static PerDevice attr;   // k_center's shared-memory limit, set once per device
+    const int ar = attr.get([]() -> int { return -(int)center_prepare_current_device(); });
+    if (ar < 0) return (cudaError_t)(-ar);
     k_center<<<1, 1024, 2 * N * sizeof(float), st>>>(arp, y, N, 30, dec);
     ISAR_COUNT(1);
     k_cut<<<M, 256, 0, st>>>(y, N, dec, cut);

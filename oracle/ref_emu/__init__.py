@@ -29,14 +29,20 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 ORACLE = os.path.dirname(HERE)
 OUT = os.path.join(ORACLE, "_ref")
 LIB = os.path.join(OUT, "libisar_ref_emu.so")
-REF_DIR = os.environ.get("ISAR_REFERENCE_DIR", "/root/reference/isar_imaging")
+# The reference checkout's isar_imaging directory comes from the environment
+# only (ISAR_REFERENCE_DIR); the recipes that build this emulation set it.
+
+
+def ref_dir():
+    return os.environ.get("ISAR_REFERENCE_DIR", "")
 REF_SOURCES = ["common.cu", "high_speed_compensation.cu", "range_alignment.cu", "phase_adjustment.cu",
                "mtrc.cu", "isar_main.cu", "isar_imaging_export.cpp"]
 _LAUNCH = re.compile(r"([A-Za-z_]\w*)\s*<<\s*<(.*)>>\s*>\s*\(")
 
 
 def reference_present():
-    return all(os.path.exists(os.path.join(REF_DIR, s)) for s in REF_SOURCES)
+    d = ref_dir()
+    return bool(d) and all(os.path.exists(os.path.join(d, s)) for s in REF_SOURCES)
 
 
 def _cuda_include():
@@ -54,7 +60,7 @@ def _flags():
          "-D__global__=", "-D__device__=", "-D__host__=", "-D__shared__=", "-D__STORAGE__=extern",
          "-D__declspec(x)=",
          "-include", os.path.join(HERE, "include", "emu_pre.h"),
-         "-I", os.path.join(HERE, "include"), "-I", REF_DIR]
+         "-I", os.path.join(HERE, "include"), "-I", ref_dir()]
     for d in _cuda_include():
         f += ["-I", d]
     return f
@@ -67,7 +73,7 @@ def transform(text):
 
 def _compile_ref(src):
     obj = os.path.join(OUT, os.path.basename(src) + ".o")
-    text = transform(open(os.path.join(REF_DIR, src), encoding="utf-8-sig").read())
+    text = transform(open(os.path.join(ref_dir(), src), encoding="utf-8-sig").read())
     cmd = ["g++"] + _flags() + ["-x", "c++", "-", "-c", "-o", obj]
     r = subprocess.run(cmd, input=text, capture_output=True, text=True)
     if r.returncode != 0:
@@ -87,7 +93,7 @@ def _compile_own(src):
 def build(force=False):
     """Builds oracle/_ref/libisar_ref_emu.so from the reference sources."""
     if not reference_present():
-        raise RuntimeError("reference sources not found under %s" % REF_DIR)
+        raise RuntimeError("reference sources not found (ISAR_REFERENCE_DIR=%r)" % ref_dir())
     if not force and os.path.exists(LIB):
         mine = [os.path.join(HERE, p) for p in ("emu_runtime.cpp", "ref_driver.cpp", "__init__.py")]
         mine += [os.path.join(HERE, "include", p) for p in os.listdir(os.path.join(HERE, "include"))]

@@ -255,6 +255,59 @@ void fft_d(std::vector<cd>& x, bool inverse)
     }
 }
 
+// Single-precision variant, selected by ISAR_EMU_FFT=float: the same radix-2
+// transform with every butterfly in float and twiddles rounded to float.  It
+// stands in for cuFFT's own FP32 arithmetic, so that the distance between the
+// reference run this way and the FP64 restatement measures how far a float
+// FFT alone moves the reference's results (its noise floor).
+using cf32 = std::complex<float>;
+
+void fft_f(std::vector<cd>& x, bool inverse)
+{
+    const int n = (int)x.size();
+    std::vector<cf32> y(n);
+    for (int i = 0; i < n; ++i) y[i] = cf32((float)x[i].real(), (float)x[i].imag());
+    for (int i = 1, j = 0; i < n; ++i) {
+        int bit = n >> 1;
+        for (; j & bit; bit >>= 1) j ^= bit;
+        j ^= bit;
+        if (i < j) std::swap(y[i], y[j]);
+    }
+    const double sgn = inverse ? 1.0 : -1.0;
+    for (int len = 2; len <= n; len <<= 1) {
+        const int half = len >> 1;
+        for (int k = 0; k < half; ++k) {
+            const double ang = sgn * 2.0 * M_PI * (double)k / (double)len;
+            const float wr = (float)std::cos(ang), wi = (float)std::sin(ang);
+            for (int s = 0; s < n; s += len) {
+                const cf32 a = y[s + k], b = y[s + k + half];
+                const float tr = __builtin_fmaf(b.real(), wr, -(b.imag() * wi));
+                const float ti = __builtin_fmaf(b.real(), wi, b.imag() * wr);
+                y[s + k + half] = cf32(a.real() - tr, a.imag() - ti);
+                y[s + k] = cf32(a.real() + tr, a.imag() + ti);
+            }
+        }
+    }
+    for (int i = 0; i < n; ++i) x[i] = cd(y[i].real(), y[i].imag());
+}
+
+bool fft_single()
+{
+    static const bool f = [] {
+        const char* e = std::getenv("ISAR_EMU_FFT");
+        return e != nullptr && std::string(e) == "float";
+    }();
+    return f;
+}
+
+void fft_any(std::vector<cd>& x, bool inverse)
+{
+    if (fft_single())
+        fft_f(x, inverse);
+    else
+        fft_d(x, inverse);
+}
+
 struct Plan {
     int n = 0, batch = 0, istride = 1, idist = 0, ostride = 1, odist = 0;
     cufftType type = CUFFT_C2C;
@@ -308,7 +361,7 @@ cufftResult cufftExecC2C(cufftHandle plan, cufftComplex* in, cufftComplex* out, 
             const cufftComplex c = in[(size_t)b * p.idist + (size_t)i * p.istride];
             v[i] = cd(c.x, c.y);
         }
-        fft_d(v, direction == CUFFT_INVERSE);
+        fft_any(v, direction == CUFFT_INVERSE);
         for (int i = 0; i < p.n; ++i)
             out[(size_t)b * p.odist + (size_t)i * p.ostride] = make_cuComplex((float)v[i].real(), (float)v[i].imag());
     }
@@ -321,7 +374,7 @@ cufftResult cufftExecR2C(cufftHandle plan, cufftReal* in, cufftComplex* out)
     std::vector<cd> v(p.n);
     for (int b = 0; b < p.batch; ++b) {
         for (int i = 0; i < p.n; ++i) v[i] = cd(in[(size_t)b * p.idist + (size_t)i * p.istride], 0.0);
-        fft_d(v, false);
+        fft_any(v, false);
         for (int i = 0; i <= p.n / 2; ++i)
             out[(size_t)b * p.odist + (size_t)i * p.ostride] = make_cuComplex((float)v[i].real(), (float)v[i].imag());
     }
@@ -340,7 +393,7 @@ cufftResult cufftExecC2R(cufftHandle plan, cufftComplex* in, cufftReal* out)
         v[0] = cd(v[0].real(), 0.0);
         v[p.n / 2] = cd(v[p.n / 2].real(), 0.0);
         for (int i = 1; i < p.n / 2; ++i) v[p.n - i] = std::conj(v[i]);
-        fft_d(v, true);
+        fft_any(v, true);
         for (int i = 0; i < p.n; ++i) out[(size_t)b * p.odist + (size_t)i * p.ostride] = (float)v[i].real();
     }
     return CUFFT_SUCCESS;

@@ -22,6 +22,8 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(os.path.dirname(HERE))
 sys.path.insert(0, ROOT)
+# the reference checkout whose sources the emulation compiles in place
+os.environ.setdefault("ISAR_REFERENCE_DIR", "/root/reference/isar_imaging")
 
 import oracle  # noqa: E402
 from oracle import ref_emu  # noqa: E402

@@ -35,6 +35,10 @@ def test_noalloc_rejects_oversized_range_num_without_gpu_work(gb300):
     assert rc == ISAR_EINVAL
     assert "8192" in gb300.last_error()
     assert lib.isar_center_cut_noalloc(None, 256, 1024, C.c_void_p(16), None) == ISAR_EINVAL
+    # pulse counts outside those of isar_create (powers of two in [128, 1024])
+    for m in (300, 64, 2048):
+        assert lib.isar_center_cut_noalloc(C.c_void_p(16), m, 1024, C.c_void_p(16), None) == ISAR_EINVAL
+        assert "echo_num" in gb300.last_error()
 
 
 @pytest.mark.gpu
@@ -42,17 +46,28 @@ def test_noalloc_center_cut_matches_context_path_two_calls_in_a_row(torch_cuda, 
     torch = torch_cuda
     lib = gb300.load()
     stream = torch.cuda.current_stream().cuda_stream
+    torch.cuda.synchronize()
+    torch_before = torch.cuda.memory_allocated()
+    # the set-up call (all arguments NULL/0) takes the scratch's address; it
+    # makes no allocation of its own
     assert lib.isar_center_cut_noalloc(None, 0, 0, None, None) == 0, gb300.last_error()
+    assert torch.cuda.memory_allocated() == torch_before
 
     cases = [(256, 8192, 11), (128, 1024, 12)]
     inputs = [_profiles_on_device(torch, gb300, M, N, seed) for M, N, seed in cases]
     outs = [torch.full((M, 1024), np.nan, dtype=torch.float32, device="cuda") for M, _, _ in cases]
+    torch.cuda.synchronize()
+    torch_before = torch.cuda.memory_allocated()
+    free_before, _ = torch.cuda.mem_get_info()
     n0 = gb300.launch_count()
     for (M, N, _), (d_y, _), d_cut in zip(cases, inputs, outs):
         rc = lib.isar_center_cut_noalloc(d_y.data_ptr(), M, N, d_cut.data_ptr(), stream)
         assert rc == 0, gb300.last_error()
     torch.cuda.synchronize()
     assert gb300.launch_count() > n0
+    # the two calls allocated nothing: neither through torch nor on the device
+    assert torch.cuda.memory_allocated() == torch_before
+    assert torch.cuda.mem_get_info()[0] == free_before
     for (M, N, _), (_, ref), d_cut in zip(cases, inputs, outs):
         got = d_cut.cpu().numpy().view(np.complex64)
         want = ref.cpu().numpy().view(np.complex64)
