@@ -4,22 +4,24 @@ alignment, centring + cut, fast minimum-entropy autofocus, CZT MTRC).
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
 
-Headline (`value`): the batched pipeline.  A step is one batch of B = 32
+Headline (`value`): the batched pipeline.  A step is one batch of B = 128
 distinct frames imaged by one CUDA graph (isar_batch_run: per-shape lanes,
-cluster-resident autofocus), inputs resident in HBM (2 GiB > L2).  Three
+cluster-resident autofocus), inputs resident in HBM (8 GiB > L2).  Three
 autofocus arms are tried in order and the first whose images pass the
-equal-entropy check is timed: (1) learned warm start + entropy stop
-criterion, (2) the stop criterion alone (Doppler-tracking start), (3) the
-reference algorithm (120 iterations).  The check: the mean final image
-entropy of the batch must not exceed the plain pipeline's by more than 1e-4.
-Every arm's check is reported.
+equal-entropy check is timed: (1) the learned warm start judged by the plain
+autofocus (the autofocus runs from the network's start and from the
+Doppler-tracking start, each until the entropy stop criterion, and keeps the
+lower final entropy), (2) the stop criterion alone (Doppler-tracking start),
+(3) the reference algorithm (120 iterations).  The check, per frame: no
+frame's final image entropy may exceed the plain pipeline's on the same frame
+by more than 1e-4.  Every arm's check is reported.
 `plain` is the single-frame pipeline (isar_image_device, the reference's
 algorithm: cooperative autofocus, 120 iterations), timed the same way.
 `e2e` goes through the public C ABI with pinned host buffers: every step
-copies its 32 echoes host->device as int16 I/Q samples (the sensor format, 4
-bytes per sample; range alignment reads them directly) and reads the 32
-images back, three buffer sets in rotation so that the copies of the next steps overlap the
-current step's compute.  Under torchrun every rank images its own frames (replicas, weak
+copies its 128 echoes host->device as int16 I/Q samples (the sensor format, 4
+bytes per sample; range alignment reads them directly) and reads the 128
+images back, three buffer sets in rotation so that the copies of the next
+steps overlap the current step's compute.  Under torchrun every rank images its own frames (replicas, weak
 scaling).
 
 --impl reference times the CPU restatement of the reference's chain (the
@@ -39,15 +41,15 @@ sys.path.insert(0, ROOT)
 
 M, N = 1024, 8192
 C = 512
-B = 32                      # frames per batch step
+B = 128                     # frames per batch step
 TOL = 3e-7                  # autofocus entropy stop criterion (relative change per iteration)
 E2E_SETS = 3                # end-to-end buffer sets in rotation (copies of later steps run ahead)
 METRIC = "frames/s @1024×8192 c64: learned+batched vs plain on 1 GB300, equal entropy"
-ARMS = [("learned warm start + entropy stop criterion", True, TOL),
+ARMS = [("learned warm start judged by the plain autofocus (both to the entropy stop criterion)", True, TOL),
         ("entropy stop criterion, Doppler-tracking start", False, TOL),
         ("reference algorithm (120 iterations)", False, 0.0)]
 WORKLOAD = ("full five-stage pipeline, 1024 pulses x 8192 range cells complex64, HPC + MTRC on, "
-            "batches of 32 frames")
+            "batches of 128 frames")
 # DRAM bytes (read + write) of one range-alignment stage at 1024 x 8192, all
 # its kernels, per frame (spectral envelope merge): dram__bytes_read.sum +
 # dram__bytes_write.sum from an ncu capture of `bench.py --profile plain`
@@ -248,11 +250,12 @@ def run_gb300(args):
 
     # first arm whose images pass the equal-entropy check (the last one is
     # the reference algorithm itself)
-    check = {"criterion": "mean(dE) <= 1e-4 against the plain pipeline", "frames": B, "arms": []}
+    check = {"criterion": "every frame: final image entropy <= the plain pipeline's + 1e-4", "frames": B,
+             "arms": []}
     for name, learned, tol in ARMS:
         tune_ms, e_batch = configure(learned, tol)
         dE = np.array(e_batch) - np.array(e_plain)
-        ok = bool(dE.mean() <= 1e-4)
+        ok = bool(dE.max() <= 1e-4)
         check["arms"].append({"arm": name, "tol": tol, "mean_dE": float(dE.mean()), "max_dE": float(dE.max()),
                               "min_dE": float(dE.min()), "frames_worse_1e-4": int((dE > 1e-4).sum()),
                               "passed": ok})
@@ -359,7 +362,7 @@ def run_gb300(args):
                 "4 deg rotation, 3000 m/s + 50 m/s^2, drift 0.5 cell, quadratic+random phase error, SNR 5 dB)",
         "config": {"workload": WORKLOAD, "pipeline": mode, "M": M, "N": N, "flags": "hpc+mtrc",
                    "batch_frames": B, "lanes": lanes, "tuning": tuning, "autotune_best_ms": tune_ms,
-                   "l2": "inputs larger than L2: 32 distinct frames x 64 MiB per step", "parallelism": "replicas"},
+                   "l2": "inputs larger than L2: 128 distinct frames x 64 MiB per step", "parallelism": "replicas"},
         "plain": {"frames_per_s": ws * 1e3 / plain_ms, "ms_per_frame": plain_ms, "stage_ms": stage_ms, "U": U,
                   "pipeline": "single frame per call, cooperative autofocus, 120 iterations"},
         "speedup_vs_plain": plain_ms * B / ms,

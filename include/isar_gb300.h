@@ -79,12 +79,17 @@ typedef struct {
     int tgt_num;              /* fastEntropy target range bins               */
     int unit2_num;            /* U, bins used by the autofocus               */
     int bins[512];            /* the U bins, ascending                       */
-    int af_iterations;        /* autofocus phase updates applied             */
+    int af_iterations;        /* autofocus phase updates applied (with a warm
+                                 start: both legs)                           */
     float af_entropy;         /* entropy of the U bins at the last evaluated
+                                 phase, with a warm start of the kept final
                                  phase (cluster engine; NaN otherwise)       */
-    int ws_used;              /* the learned warm start was kept             */
-    float af_entropy_start[2];/* entropy of the Doppler start and of the
-                                 learned start (NaN without a warm start)    */
+    int ws_used;              /* the learned leg's result was kept           */
+    float af_entropy_final[2];/* final entropy of the U bins of the plain leg
+                                 (Doppler-tracking start) and of the learned
+                                 leg (NaN without a warm start)              */
+    int af_iterations_leg[2]; /* phase updates of the plain and the learned
+                                 leg (0 without a warm start)                */
 } isar_trace;
 
 /*
@@ -223,6 +228,15 @@ ISAR_API int isar_synth_device(const isar_synth_params* p, float* d_out, double*
  * operation.  Isolates the rest of the chain from the float rounding of the
  * reference's parabolic shift estimate in parity tests. */
 ISAR_API int isar_set_ra_shifts(isar_ctx* ctx, const float* shifts);
+
+/* Test hook for the bounded device waits that replace the reference's
+ * exit() on a CUDA error (helper_cuda.h:583-595): the cooperative autofocus
+ * engine's grid barrier gives up after `polls` polls (0 = the default limit,
+ * about a second) and, with never_complete != 0, waits for one arrival more
+ * than the grid makes, so that every CTA gives up, sets the timeout flag and
+ * leaves the kernel.  The frame then reports ISAR_ECUDA and the context stays
+ * usable.  (0, 0) restores normal operation. */
+ISAR_API int isar_test_barrier_timeout(isar_ctx* ctx, unsigned polls, int never_complete);
 
 /*
  * HRRPCenter + cutRangeProfile without a context and without allocating:

@@ -31,7 +31,8 @@ EXPORTS = ("isar_get_last_error", "isar_version", "isar_create", "isar_destroy",
            "isar_image_host", "isar_image_device", "isar_get_trace", "isar_stage_hpc",
            "isar_stage_range_align", "isar_stage_center_cut", "isar_stage_fast_entropy",
            "isar_stage_post", "isar_fft_rows", "isar_get_profiles", "isar_synth_device", "isar_launch_count",
-           "isar_synchronize", "isar_set_ra_shifts", "isar_center_cut_noalloc", "isar_get_tuning",
+           "isar_synchronize", "isar_set_ra_shifts", "isar_test_barrier_timeout", "isar_center_cut_noalloc",
+           "isar_get_tuning",
            "isar_set_tuning", "isar_autotune", "isar_batch_create", "isar_batch_destroy", "isar_batch_stream",
            "isar_batch_run", "isar_batch_synchronize", "isar_batch_set_tuning", "isar_batch_get_tuning",
            "isar_batch_lanes", "isar_batch_autotune", "isar_wsnet_param_count", "isar_wsnet_create",
@@ -65,7 +66,8 @@ class Trace(C.Structure):
                 ("center_shift", C.c_int), ("cut_offset", C.c_int), ("center_idx1_len", C.c_int),
                 ("center_idx2_len", C.c_int), ("center_threshold", C.c_float), ("tgt_num", C.c_int),
                 ("unit2_num", C.c_int), ("bins", C.c_int * 512), ("af_iterations", C.c_int),
-                ("af_entropy", C.c_float), ("ws_used", C.c_int), ("af_entropy_start", C.c_float * 2)]
+                ("af_entropy", C.c_float), ("ws_used", C.c_int), ("af_entropy_final", C.c_float * 2),
+                ("af_iterations_leg", C.c_int * 2)]
 
 
 class Tuning(C.Structure):
@@ -120,6 +122,7 @@ def load(build_if_missing=True):
         "isar_launch_count": (C.c_longlong, []),
         "isar_synchronize": (i, [vp]),
         "isar_set_ra_shifts": (i, [vp, vp]),
+        "isar_test_barrier_timeout": (i, [vp, C.c_uint, i]),
         "isar_center_cut_noalloc": (i, [vp, i, i, vp, vp]),
         "isar_get_tuning": (i, [vp, C.POINTER(Tuning)]),
         "isar_set_tuning": (i, [vp, C.POINTER(Tuning)]),
@@ -290,6 +293,12 @@ class Context:
         self._given = np.ascontiguousarray(shifts, np.float32)
         _check(self._lib.isar_set_ra_shifts(self._h, self._given.ctypes.data), "isar_set_ra_shifts")
 
+    def test_barrier_timeout(self, polls=0, never_complete=False):
+        """Test hook: the autofocus grid barrier polls at most `polls` times
+        and, with never_complete, waits for an arrival that never comes."""
+        _check(self._lib.isar_test_barrier_timeout(self._h, int(polls), int(bool(never_complete))),
+               "isar_test_barrier_timeout")
+
     def synchronize(self):
         _check(self._lib.isar_synchronize(self._h), "isar_synchronize")
 
@@ -312,7 +321,8 @@ class Context:
                     center_idx2_len=t.center_idx2_len, center_threshold=t.center_threshold,
                     tgt_num=t.tgt_num, unit2_num=U, bins=np.array(t.bins[:min(U, 512)], np.int32),
                     af_iterations=t.af_iterations, af_entropy=t.af_entropy, ws_used=t.ws_used,
-                    af_entropy_start=(t.af_entropy_start[0], t.af_entropy_start[1]))
+                    af_entropy_final=(t.af_entropy_final[0], t.af_entropy_final[1]),
+                    af_iterations_leg=(t.af_iterations_leg[0], t.af_iterations_leg[1]))
 
     def tuning(self):
         t = Tuning()

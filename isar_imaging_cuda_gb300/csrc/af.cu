@@ -328,12 +328,11 @@ k_fe_select(const double* __restrict__ E, const double* __restrict__ H, int* __r
 }
 
 // Grid-wide barrier for cooperative launches (all CTAs co-resident): arrive
-// on a monotonic counter and wait, with a bounded number of polls, until it
-// reaches `target`.  A timeout sets *err and makes every later barrier fail
-// fast, so that all CTAs leave the kernel.  Returns false on failure.
-constexpr unsigned long long kSpinLimit = 1ull << 22;
-
-__device__ __forceinline__ bool grid_barrier(unsigned* count, unsigned target, int* err)
+// on a monotonic counter and wait, with at most `limit` polls (kSpinLimit,
+// about a second), until it reaches `target`.  A timeout sets *err and makes
+// every later barrier fail fast, so that all CTAs leave the kernel.  Returns
+// false on failure.
+__device__ __forceinline__ bool grid_barrier(unsigned* count, unsigned target, int* err, unsigned long long limit)
 {
     __shared__ int s_ok;
     __syncthreads();
@@ -348,7 +347,7 @@ __device__ __forceinline__ bool grid_barrier(unsigned* count, unsigned target, i
                 ok = 0;
                 break;
             }
-            if (++spins > kSpinLimit) {
+            if (++spins > limit) {
                 atomicExch(err, 1);
                 ok = 0;
                 break;
@@ -373,7 +372,8 @@ __device__ __forceinline__ bool grid_barrier(unsigned* count, unsigned target, i
 template <int M>
 __global__ void __launch_bounds__(4 * (M / 16))
 k_af_persist(const float2* __restrict__ cut, const int* __restrict__ bins, const int* __restrict__ fdec,
-             float2* phase, float2* P, unsigned* bar, int* err, int iters, const float2* __restrict__ tw)
+             float2* phase, float2* P, unsigned* bar, int* err, int iters, const float2* __restrict__ tw,
+             BarrierTest bt)
 {
     using F = FFTShape<M>;
     constexpr int TEAMS = 4;
@@ -423,7 +423,7 @@ k_af_persist(const float2* __restrict__ cut, const int* __restrict__ bins, const
                 __stcg(&P[(size_t)m * G + blockIdx.x], s);
             }
         }
-        if (!grid_barrier(bar, (unsigned)(2 * it + 1) * G, err)) return;
+        if (!grid_barrier(bar, (unsigned)(2 * it + 1) * G + bt.extra, err, bt.limit)) return;
         for (int m = blockIdx.x + warp * G; m < M; m += nwarp * G) {
             float2 s = make_float2(0.0f, 0.0f);
             for (int b = lane; b < nact; b += 32) {
@@ -441,7 +441,7 @@ k_af_persist(const float2* __restrict__ cut, const int* __restrict__ bins, const
                 __stcg(&phase[m], make_float2(s.x / a, s.y / a));
             }
         }
-        if (!grid_barrier(bar, (unsigned)(2 * it + 2) * G, err)) return;
+        if (!grid_barrier(bar, (unsigned)(2 * it + 2) * G + bt.extra, err, bt.limit)) return;
     }
 }
 
@@ -481,12 +481,22 @@ struct AFFrame {
     const float2* cut;     // [M][512]
     const int* bins;       // [U]
     const int* fdec;       // [1] = U
-    float2* phase;         // [M] in: start phase, out: final phase
-    int* stat;             // [0] iterations applied, [1] entropy bits, [2] alt start used,
-                           // [3], [4] entropy bits of the two starts; may be null
-    const float2* alt;     // [M] second start phase (learned warm start) or null
+    float2* phase;         // [M] in: Doppler-tracking start phase, out: final phase
+    int* stat;             // [0] iterations applied (both legs), [1] final entropy bits,
+                           // [2] learned leg kept, [3], [4] final entropy bits of the
+                           // Doppler and learned legs, [5], [6] their iterations;
+                           // may be null
+    float2* alt;           // [M] learned start phase in, the learned leg's final phase
+                           // out (warm start), or null
     float2* gcol;          // [U][M] scratch: contiguous copy of the bin columns
 };
+
+// With a learned start (AFFrame::alt), both cluster engines run two legs: the
+// autofocus from the learned start until the stop criterion, then from the
+// Doppler-tracking start until the same criterion (the plain autofocus), and
+// keep the final phase whose entropy of the selected bins is lower.  The
+// autofocus is the judge: a frame on which the learned start ends worse
+// reverts to the plain result.
 
 template <int M>
 __global__ void __launch_bounds__(AFC<M>::THREADS, 1)
@@ -588,75 +598,13 @@ k_af_cluster(AFFrame f, int iters, float tol, const float2* __restrict__ tw)
         }
     };
 
-    // Optional second start (learned warm start): keep whichever of the two
-    // starting phases has the lower entropy of the selected bins.
-    if (f.alt) {
-        float e_start[2];
-#pragma unroll 1
-        for (int k = 0; k < 2; ++k) {
-            if (k == 1) {
-                __syncthreads();
-                for (int m = tid; m < M; m += A::THREADS) ph[m] = f.alt[m];
-            }
-            float s1 = 0.0f, s2 = 0.0f;
-            sweep(false, true, s1, s2);
-#pragma unroll
-            for (int o = 16; o > 0; o >>= 1) {
-                s1 += __shfl_xor_sync(0xffffffffu, s1, o);
-                s2 += __shfl_xor_sync(0xffffffffu, s2, o);
-            }
-            if (lane == 0) {
-                red[warp] = s1;
-                red[16 + warp] = s2;
-            }
-            __syncthreads();
-            if (tid == 0) {
-                double a1 = 0.0, a2 = 0.0;
-                for (int w = 0; w < A::THREADS / 32; ++w) {
-                    a1 += red[w];
-                    a2 += red[16 + w];
-                }
-                red[32] = a1;
-                red[33] = a2;
-            }
-            cl.sync();
-            if (tid == 0) {
-                double S1 = 0.0, S2 = 0.0;
-                for (int q = 0; q < CL; ++q) {
-                    const double* rr = cl.map_shared_rank(red, q);
-                    S1 += rr[32];
-                    S2 += rr[33];
-                }
-                red[41 + k] = logf((float)S1) - kLn2 * (float)S2 / (float)S1;
-            }
-            cl.sync();
-            e_start[k] = (float)red[41 + k];
-        }
-        const bool use_alt = e_start[1] < e_start[0];
-        if (!use_alt) {
-            __syncthreads();
-            for (int m = tid; m < M; m += A::THREADS) ph[m] = f.phase[m];
-        }
-        if (r == 0 && tid == 0 && f.stat) {
-            f.stat[2] = use_alt ? 1 : 0;
-            f.stat[3] = __float_as_int(e_start[0]);
-            f.stat[4] = __float_as_int(e_start[1]);
-        }
-        __syncthreads();
-    }
-
-    float e_prev = 0.0f, e_last = 0.0f;   // meaningful in thread 0
-    int used = iters;
-#pragma unroll 1
-    for (int it = 0; it < iters; ++it) {
-        // the entropy is needed by the stop criterion, and for the trace at
-        // the last iteration; elsewhere its logarithms are skipped
-        const bool check = tol > 0.0f && it % kStopEvery == 0;
-        const bool need_e = check || it == iters - 1;
-        float s1 = 0.0f, s2 = 0.0f;
-        sweep(true, need_e, s1, s2);
-        // Entropy sums: float per warp, double per CTA (red[32..33]) and per
-        // cluster, all by one thread (FP64 is slow on this part).
+    // Entropy of the selected bins from the per-thread sums of one sweep:
+    // float per warp, double per CTA (red[32..33]) and per cluster, by thread
+    // 0 of every CTA in the same order (FP64 is slow on this part).  The
+    // cluster barrier inside publishes red[32..33]; the caller's next cluster
+    // barrier must come before they are rewritten.  Returns the value in
+    // thread 0.
+    auto entropy_sums = [&](float s1, float s2) {
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) {
             s1 += __shfl_xor_sync(0xffffffffu, s1, o);
@@ -677,6 +625,7 @@ k_af_cluster(AFFrame f, int iters, float tol, const float2* __restrict__ tw)
             red[33] = a2;
         }
         cl.sync();
+        float E = 0.0f;
         if (tid == 0) {
             double S1 = 0.0, S2 = 0.0;
             for (int q = 0; q < CL; ++q) {
@@ -684,53 +633,116 @@ k_af_cluster(AFFrame f, int iters, float tol, const float2* __restrict__ tw)
                 S1 += rr[32];
                 S2 += rr[33];
             }
-            bool stop = false;
-            if (need_e) {
-                const float E = logf((float)S1) - kLn2 * (float)S2 / (float)S1;
-                if (check) {
-                    stop = it > 0 && fabsf(E - e_prev) <= (float)kStopEvery * tol * fabsf(E);
-                    e_prev = E;
-                }
-                e_last = E;
-            }
-            red[40] = stop ? 1.0 : 0.0;
+            E = logf((float)S1) - kLn2 * (float)S2 / (float)S1;
         }
-        // This CTA's rows [r*rows, (r+1)*rows) of every CTA's partial sums,
-        // gathered with independent remote loads into buf[q][row] (behind P).
-        float2* buf = smb + M;
-        for (int idx = tid; idx < CL * rows; idx += A::THREADS) {
-            const int q = idx / rows, ml = idx - q * rows;
-            buf[idx] = cl.map_shared_rank(P, q)[r * rows + ml];
-        }
-        __syncthreads();
-        const bool stop = red[40] != 0.0;
-        if (!stop) {
-            for (int ml = tid; ml < rows; ml += A::THREADS) {
-                float2 s = make_float2(0.0f, 0.0f);
-                for (int q = 0; q < CL; ++q) {
-                    const float2 v = buf[q * rows + ml];
-                    s.x += v.x;
-                    s.y += v.y;
+        return E;
+    };
+
+    // One autofocus run from the phase in ph: up to `iters` updates, fewer
+    // when the stop criterion ends it.  Returns (in thread 0) the entropy at
+    // the last evaluated phase or, with want_final, of the final phase (one
+    // more entropy sweep when all `iters` updates were applied).
+    auto leg = [&](bool want_final, int& used) -> float {
+        float e_prev = 0.0f, e_last = 0.0f;   // meaningful in thread 0
+        bool stopped = false;
+        used = iters;
+#pragma unroll 1
+        for (int it = 0; it < iters; ++it) {
+            // the entropy is needed by the stop criterion, and for the trace at
+            // the last iteration; elsewhere its logarithms are skipped
+            const bool check = tol > 0.0f && it % kStopEvery == 0;
+            const bool need_e = check || it == iters - 1;
+            float s1 = 0.0f, s2 = 0.0f;
+            sweep(true, need_e, s1, s2);
+            const float E = entropy_sums(s1, s2);
+            if (tid == 0) {
+                bool stop = false;
+                if (need_e) {
+                    if (check) {
+                        stop = it > 0 && fabsf(E - e_prev) <= (float)kStopEvery * tol * fabsf(E);
+                        e_prev = E;
+                    }
+                    e_last = E;
                 }
-                const float a = sqrtf(s.x * s.x + s.y * s.y);
-                buf[CL * rows + ml] = make_float2(s.x / a, s.y / a);
+                red[40] = stop ? 1.0 : 0.0;
             }
-            __syncthreads();
+            // This CTA's rows [r*rows, (r+1)*rows) of every CTA's partial sums,
+            // gathered with independent remote loads into buf[q][row] (behind P).
+            float2* buf = smb + M;
             for (int idx = tid; idx < CL * rows; idx += A::THREADS) {
                 const int q = idx / rows, ml = idx - q * rows;
-                cl.map_shared_rank(ph, q)[r * rows + ml] = buf[CL * rows + ml];
+                buf[idx] = cl.map_shared_rank(P, q)[r * rows + ml];
+            }
+            __syncthreads();
+            const bool stop = red[40] != 0.0;
+            if (!stop) {
+                for (int ml = tid; ml < rows; ml += A::THREADS) {
+                    float2 s = make_float2(0.0f, 0.0f);
+                    for (int q = 0; q < CL; ++q) {
+                        const float2 v = buf[q * rows + ml];
+                        s.x += v.x;
+                        s.y += v.y;
+                    }
+                    const float a = sqrtf(s.x * s.x + s.y * s.y);
+                    buf[CL * rows + ml] = make_float2(s.x / a, s.y / a);
+                }
+                __syncthreads();
+                for (int idx = tid; idx < CL * rows; idx += A::THREADS) {
+                    const int q = idx / rows, ml = idx - q * rows;
+                    cl.map_shared_rank(ph, q)[r * rows + ml] = buf[CL * rows + ml];
+                }
+            }
+            cl.sync();
+            if (stop) {
+                used = it;
+                stopped = true;
+                break;
             }
         }
-        cl.sync();
-        if (stop) {
-            used = it;
-            break;
+        if (want_final && !stopped) {
+            float s1 = 0.0f, s2 = 0.0f;
+            sweep(false, true, s1, s2);
+            const float E = entropy_sums(s1, s2);
+            if (tid == 0) e_last = E;
+            cl.sync();   // red[32..33] are read remotely before a later sweep rewrites them
         }
+        return e_last;
+    };
+
+    if (!f.alt) {
+        int used;
+        const float e = leg(false, used);
+        for (int m = r * rows + tid; m < (r + 1) * rows; m += A::THREADS) f.phase[m] = ph[m];
+        if (r == 0 && tid == 0 && f.stat) {
+            f.stat[0] = used;
+            f.stat[1] = __float_as_int(e);
+        }
+        return;
     }
-    for (int m = r * rows + tid; m < (r + 1) * rows; m += A::THREADS) f.phase[m] = ph[m];
+    // learned leg, then the plain leg from the Doppler-tracking start; the
+    // lower final entropy is kept
+    __syncthreads();
+    for (int m = tid; m < M; m += A::THREADS) ph[m] = f.alt[m];
+    __syncthreads();
+    int used_l, used_d;
+    const float e_l = leg(true, used_l);
+    for (int m = r * rows + tid; m < (r + 1) * rows; m += A::THREADS) f.alt[m] = ph[m];
+    __syncthreads();
+    for (int m = tid; m < M; m += A::THREADS) ph[m] = f.phase[m];
+    __syncthreads();
+    const float e_d = leg(true, used_d);
+    if (tid == 0) red[43] = e_l < e_d ? 1.0 : 0.0;
+    __syncthreads();
+    const bool keep_l = red[43] != 0.0;
+    for (int m = r * rows + tid; m < (r + 1) * rows; m += A::THREADS) f.phase[m] = keep_l ? f.alt[m] : ph[m];
     if (r == 0 && tid == 0 && f.stat) {
-        f.stat[0] = used;
-        f.stat[1] = __float_as_int(e_last);
+        f.stat[0] = used_l + used_d;
+        f.stat[1] = __float_as_int(keep_l ? e_l : e_d);
+        f.stat[2] = keep_l ? 1 : 0;
+        f.stat[3] = __float_as_int(e_d);
+        f.stat[4] = __float_as_int(e_l);
+        f.stat[5] = used_d;
+        f.stat[6] = used_l;
     }
 }
 
@@ -917,103 +929,117 @@ k_af_cluster_w1024(AFFrame f, int iters, float tol, const float2* __restrict__ t
         return logf((float)S1) - kLn2 * (float)S2 / (float)S1;
     };
 
-    if (f.alt) {
-        float e_start[2];
-#pragma unroll 1
-        for (int k = 0; k < 2; ++k) {
-            if (k == 1) {
-                __syncthreads();
-                for (int m = tid; m < M; m += AFW::THREADS) ph[m] = f.alt[m];
-                __syncthreads();
-            }
-            float s1 = 0.0f, s2 = 0.0f;
-            sweep(false, true, s1, s2);
-            entropy_part(s1, s2);
-            cl.sync();
-            if (warp == 0) {
-                const float E = entropy_total();
-                if (lane == 0) red[41 + k] = E;
-            }
-            cl.sync();   // red[32..33] are read remotely before the next sweep rewrites them
-            e_start[k] = (float)red[41 + k];
-        }
-        const bool use_alt = e_start[1] < e_start[0];
-        if (!use_alt) {
-            __syncthreads();
-            for (int m = tid; m < M; m += AFW::THREADS) ph[m] = f.phase[m];
-        }
-        if (r == 0 && tid == 0 && f.stat) {
-            f.stat[2] = use_alt ? 1 : 0;
-            f.stat[3] = __float_as_int(e_start[0]);
-            f.stat[4] = __float_as_int(e_start[1]);
-        }
-        __syncthreads();
-    }
-
-    float e_prev = 0.0f, e_last = 0.0f;   // meaningful in thread 0
-    int used = iters;
-    int lg_rows = 0;
-    while ((1 << lg_rows) < rows) ++lg_rows;
+    // One autofocus run from the phase in ph (see k_af_cluster): returns, in
+    // warp 0, the entropy at the last evaluated phase or, with want_final, of
+    // the final phase.
     float2* buf = tiles + AFW::TILE;   // behind P (tile 0 holds P)
+    auto leg = [&](bool want_final, int& used) -> float {
+        float e_prev = 0.0f, e_last = 0.0f;   // meaningful in warp 0
+        bool stopped = false;
+        used = iters;
+        int lg_rows = 0;
+        while ((1 << lg_rows) < rows) ++lg_rows;
 #pragma unroll 1
-    for (int it = 0; it < iters; ++it) {
-        // the entropy is needed by the stop criterion or for the last trace
-        const bool check = tol > 0.0f && it % kStopEvery == 0;
-        const bool need_e = check || it == iters - 1;
-        float s1 = 0.0f, s2 = 0.0f;
-        sweep(true, need_e, s1, s2);
-        if (need_e) entropy_part(s1, s2);
-        cl.sync();   // P and red[32..33] of every CTA are complete
-        if (warp == 0) {
-            bool stop = false;
-            if (need_e) {
-                const float E = entropy_total();
-                if (check) {
-                    stop = it > 0 && fabsf(E - e_prev) <= (float)kStopEvery * tol * fabsf(E);
-                    e_prev = E;
+        for (int it = 0; it < iters; ++it) {
+            // the entropy is needed by the stop criterion or for the last trace
+            const bool check = tol > 0.0f && it % kStopEvery == 0;
+            const bool need_e = check || it == iters - 1;
+            float s1 = 0.0f, s2 = 0.0f;
+            sweep(true, need_e, s1, s2);
+            if (need_e) entropy_part(s1, s2);
+            cl.sync();   // P and red[32..33] of every CTA are complete
+            if (warp == 0) {
+                bool stop = false;
+                if (need_e) {
+                    const float E = entropy_total();
+                    if (check) {
+                        stop = it > 0 && fabsf(E - e_prev) <= (float)kStopEvery * tol * fabsf(E);
+                        e_prev = E;
+                    }
+                    e_last = E;
                 }
-                e_last = E;
+                if (lane == 0) red[40] = stop ? 1.0 : 0.0;
             }
-            if (lane == 0) red[40] = stop ? 1.0 : 0.0;
-        }
-        // this CTA's rows of the cluster sum: slice r of every CTA's P
-#pragma unroll
-        for (int i = 0; i < M / AFW::THREADS; ++i) {
-            const int idx = tid + i * AFW::THREADS;
-            const int q = idx >> lg_rows, ml = idx & (rows - 1);
-            buf[idx] = cl.map_shared_rank(P, q)[r * rows + ml];
-        }
-        __syncthreads();
-        const bool stop = red[40] != 0.0;
-        if (!stop) {
-            for (int ml = tid; ml < rows; ml += AFW::THREADS) {
-                float2 s = make_float2(0.0f, 0.0f);
-                for (int q = 0; q < CL; ++q) {
-                    const float2 v = buf[q * rows + ml];
-                    s.x += v.x;
-                    s.y += v.y;
-                }
-                const float a = sqrtf(s.x * s.x + s.y * s.y);
-                buf[M + ml] = make_float2(s.x / a, s.y / a);
-            }
-            __syncthreads();
+            // this CTA's rows of the cluster sum: slice r of every CTA's P
 #pragma unroll
             for (int i = 0; i < M / AFW::THREADS; ++i) {
                 const int idx = tid + i * AFW::THREADS;
                 const int q = idx >> lg_rows, ml = idx & (rows - 1);
-                cl.map_shared_rank(ph, q)[r * rows + ml] = buf[M + ml];
+                buf[idx] = cl.map_shared_rank(P, q)[r * rows + ml];
+            }
+            __syncthreads();
+            const bool stop = red[40] != 0.0;
+            if (!stop) {
+                for (int ml = tid; ml < rows; ml += AFW::THREADS) {
+                    float2 s = make_float2(0.0f, 0.0f);
+                    for (int q = 0; q < CL; ++q) {
+                        const float2 v = buf[q * rows + ml];
+                        s.x += v.x;
+                        s.y += v.y;
+                    }
+                    const float a = sqrtf(s.x * s.x + s.y * s.y);
+                    buf[M + ml] = make_float2(s.x / a, s.y / a);
+                }
+                __syncthreads();
+#pragma unroll
+                for (int i = 0; i < M / AFW::THREADS; ++i) {
+                    const int idx = tid + i * AFW::THREADS;
+                    const int q = idx >> lg_rows, ml = idx & (rows - 1);
+                    cl.map_shared_rank(ph, q)[r * rows + ml] = buf[M + ml];
+                }
+            }
+            cl.sync();
+            if (stop) {
+                used = it;
+                stopped = true;
+                break;
             }
         }
-        cl.sync();
-        if (stop) {
-            used = it;
-            break;
+        if (want_final && !stopped) {
+            float s1 = 0.0f, s2 = 0.0f;
+            sweep(false, true, s1, s2);
+            entropy_part(s1, s2);
+            cl.sync();
+            if (warp == 0) e_last = entropy_total();
+            cl.sync();   // red[32..33] are read remotely before a later sweep rewrites them
         }
+        return e_last;
+    };
+
+    if (!f.alt) {
+        int used;
+        const float e = leg(false, used);
+        for (int m = r * rows + tid; m < (r + 1) * rows; m += AFW::THREADS) f.phase[m] = ph[m];
+        if (r == 0 && tid == 0 && f.stat) {
+            f.stat[0] = used;
+            f.stat[1] = __float_as_int(e);
+        }
+        return;
     }
-    for (int m = r * rows + tid; m < (r + 1) * rows; m += AFW::THREADS) f.phase[m] = ph[m];
+    // learned leg, then the plain leg from the Doppler-tracking start; the
+    // lower final entropy is kept (see AFFrame)
+    __syncthreads();
+    for (int m = tid; m < M; m += AFW::THREADS) ph[m] = f.alt[m];
+    __syncthreads();
+    int used_l, used_d;
+    const float e_l = leg(true, used_l);
+    for (int m = r * rows + tid; m < (r + 1) * rows; m += AFW::THREADS) f.alt[m] = ph[m];
+    __syncthreads();
+    for (int m = tid; m < M; m += AFW::THREADS) ph[m] = f.phase[m];
+    __syncthreads();
+    const float e_d = leg(true, used_d);
+    if (tid == 0) red[43] = e_l < e_d ? 1.0 : 0.0;
+    __syncthreads();
+    const bool keep_l = red[43] != 0.0;
+    for (int m = r * rows + tid; m < (r + 1) * rows; m += AFW::THREADS) f.phase[m] = keep_l ? f.alt[m] : ph[m];
     if (r == 0 && tid == 0 && f.stat) {
-        f.stat[0] = used;
-        f.stat[1] = __float_as_int(e_last);
+        f.stat[0] = used_l + used_d;
+        f.stat[1] = __float_as_int(keep_l ? e_l : e_d);
+        f.stat[2] = keep_l ? 1 : 0;
+        f.stat[3] = __float_as_int(e_d);
+        f.stat[4] = __float_as_int(e_l);
+        f.stat[5] = used_d;
+        f.stat[6] = used_l;
     }
 }
 
@@ -1192,8 +1218,9 @@ static cudaError_t fe_run_m(const FEArgs& a, cudaStream_t st)
         int* err = reinterpret_cast<int*>(a.bar + 1);
         int iters = a.iters;
         const float2* tw = a.tw;
+        BarrierTest bt = a.bar_test;
         void* args[] = {(void*)&cut, (void*)&bins, (void*)&fdec, (void*)&phase, (void*)&P,
-                        (void*)&bar, (void*)&err, (void*)&iters, (void*)&tw};
+                        (void*)&bar, (void*)&err, (void*)&iters, (void*)&tw, (void*)&bt};
         if ((e = cudaLaunchCooperativeKernel((const void*)k_af_persist<M>, dim3(grid_p), dim3(4 * F::T), args, smem_p,
                                              st)))
             return e;

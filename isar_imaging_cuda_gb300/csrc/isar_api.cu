@@ -182,6 +182,7 @@ struct isar_ctx {
     std::vector<void*> allocs;
     double hpc_coef_over_fs2 = 0.0;
     bool ra_given = false;         // range alignment uses injected shifts (test hook)
+    isar::BarrierTest bar_test;    // autofocus grid-barrier poll limit (test hook)
     // tuning (isar_set_tuning / the autotuner); defaults as the reference
     int ra_rows_each_level = 0;    // 0: spectral envelope merge
     int ra_pair_min = 128;
@@ -384,6 +385,7 @@ isar::FEArgs fe_args(isar_ctx* c, float2* cut, int iters)
     a.sig_part = c->d_sig_part;
     a.gcol = c->d_gcol;
     a.bar = c->d_bar;
+    a.bar_test = c->bar_test;
     a.tw = c->d_tw;
     a.af_cluster = c->af_cluster;
     a.tol = c->af_tol;
@@ -644,6 +646,18 @@ ISAR_API int isar_set_ra_shifts(isar_ctx* c, const float* shifts)
     return ISAR_OK;
 }
 
+ISAR_API int isar_test_barrier_timeout(isar_ctx* c, unsigned polls, int never_complete)
+{
+    TRY(check_ctx(c));
+    if (polls == 0 && never_complete) return fail(ISAR_EINVAL, "a barrier that never completes needs a poll limit");
+    CU(cudaStreamSynchronize(c->st));
+    c->bar_test.limit = polls ? polls : isar::kSpinLimit;
+    c->bar_test.extra = never_complete ? 1u : 0u;
+    for (auto& g : c->graphs) cudaGraphExecDestroy(g.exec);   // graphs bake the kernel arguments in
+    c->graphs.clear();
+    return ISAR_OK;
+}
+
 ISAR_API int isar_image_device(isar_ctx* c, const float* d_echo, const double* d_velocity, int flags, float* d_img)
 {
     TRY(check_ctx(c));
@@ -728,10 +742,13 @@ ISAR_API int isar_get_trace(isar_ctx* c, isar_trace* t)
     }
     t->ws_used = c->ws_w ? fdec[6] : 0;
     if (c->ws_w) {
-        std::memcpy(&t->af_entropy_start[0], &fdec[7], sizeof(float));
-        std::memcpy(&t->af_entropy_start[1], &fdec[8], sizeof(float));
+        std::memcpy(&t->af_entropy_final[0], &fdec[7], sizeof(float));
+        std::memcpy(&t->af_entropy_final[1], &fdec[8], sizeof(float));
+        t->af_iterations_leg[0] = fdec[9];
+        t->af_iterations_leg[1] = fdec[10];
     } else {
-        t->af_entropy_start[0] = t->af_entropy_start[1] = NAN;
+        t->af_entropy_final[0] = t->af_entropy_final[1] = NAN;
+        t->af_iterations_leg[0] = t->af_iterations_leg[1] = 0;
     }
     return ISAR_OK;
 }

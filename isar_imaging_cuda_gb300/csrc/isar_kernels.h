@@ -83,6 +83,15 @@ struct RAArgs {
     int x_iq16;              // x holds int16 I/Q pairs (level 0 reads them directly)
 };
 
+// Poll limit of the autofocus grid barrier (about a second of polling), and
+// the test hook that makes it run out: `extra` arrivals are added to every
+// barrier's target, so no CTA can pass and each gives up after `limit` polls.
+constexpr unsigned long long kSpinLimit = 1ull << 22;
+struct BarrierTest {
+    unsigned long long limit = kSpinLimit;
+    unsigned extra = 0;
+};
+
 struct FEArgs {
     int M;
     int iters;
@@ -97,6 +106,7 @@ struct FEArgs {
     float2* sig_part;        // [M][128] autofocus partial row sums
     float2* gcol;            // [512][M] gathered bin columns (cluster engine, M = 1024)
     unsigned* bar;           // [0] grid-barrier counter, [1] barrier timeout flag
+    BarrierTest bar_test;    // poll limit and target offset of the grid barrier
     const float2* tw;
     // Autofocus engine: 0 = one cooperative grid (128 CTAs, grid barriers);
     // 4, 8 or 16 = one thread-block cluster of that many CTAs per frame

@@ -125,6 +125,10 @@ def lib():
                                    C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
         _lib.ref_hrrp.restype = C.c_int
         _lib.ref_hrrp.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_void_p]
+        _lib.ref_parse.restype = C.c_int
+        _lib.ref_parse.argtypes = [C.c_char_p, C.c_int, C.c_int, C.c_char_p]
+        _lib.ref_extract.restype = C.c_int
+        _lib.ref_extract.argtypes = [C.c_char_p, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_char_p]
         _lib.ref_pulse_compress.restype = C.c_int
         _lib.ref_pulse_compress.argtypes = [C.c_void_p, C.c_int, C.c_double, C.c_longlong, C.c_longlong,
                                             C.c_double, C.c_longlong, C.c_void_p]
@@ -166,6 +170,43 @@ def pulse_compress(ad, velocity, B, fc, Tp, Fs):
             raise RuntimeError("reference pulse compression failed (rc=%d)" % rc)
         out[p] = o
     return out
+
+
+def read_dump(path, dtypes):
+    """Count-prefixed arrays written by the drivers' dump(): per array an
+    int64 element count, then the elements (dtypes in order)."""
+    out = []
+    with open(path, "rb") as f:
+        for dt in dtypes:
+            n = int(np.frombuffer(f.read(8), np.int64)[0])
+            out.append(np.frombuffer(f.read(n * np.dtype(dt).itemsize), dt).copy())
+    return out
+
+
+def parse(directory, polar_type=1, data_type=2):
+    """dataParsing by the reference on the .wbd files in `directory`: returns
+    (frame_len, frame_num, dataN float64, turnAngle float32)."""
+    out = os.path.join(OUT, "parse_%d.bin" % os.getpid())
+    rc = lib().ref_parse(directory.encode(), polar_type, data_type, out.encode())
+    if rc != 0:
+        raise RuntimeError("reference dataParsing failed (rc=%d)" % rc)
+    fl, dn, ta = read_dump(out, (np.int32, np.float64, np.float32))
+    os.remove(out)
+    return int(fl[0]), int(fl[1]), dn, ta
+
+
+def extract(directory, window_len, window_head, sampling_stride=1, polar_type=1, data_type=2):
+    """dataParsing + imagingMemInit + one dataExtracting by the reference:
+    returns (dataWFileSn int32, dataNOut float64, turnAngleOut float32,
+    dataW complex64)."""
+    out = os.path.join(OUT, "extract_%d.bin" % os.getpid())
+    rc = lib().ref_extract(directory.encode(), polar_type, data_type, window_len, window_head, sampling_stride,
+                           out.encode())
+    if rc != 0:
+        raise RuntimeError("reference dataExtracting failed (rc=%d)" % rc)
+    sn, dn, ta, dw = read_dump(out, (np.int32, np.float64, np.float32, np.float32))
+    os.remove(out)
+    return sn, dn, ta, dw.view(np.complex64)
 
 
 def hrrp(echo, data_type=2):

@@ -2,7 +2,10 @@
 // ONLY).  Compiled together with the reference's own sources; drives its
 // exported imaging path and its stage functions on host buffers.
 #include <complex>
+#include <cstdint>
+#include <cstdio>
 #include <cstring>
+#include <string>
 #include <vector>
 
 #include "isar_imaging_export.h"
@@ -17,7 +20,72 @@ extern double* d_velocity;
 extern float* d_hamming;
 extern cuComplex* d_hrrp;
 
+namespace {
+// Count-prefixed arrays: per array an int64 element count, then the elements.
+template <class T>
+void dump(FILE* f, const T* p, size_t n)
+{
+    const int64_t c = (int64_t)n;
+    std::fwrite(&c, sizeof(c), 1, f);
+    if (n) std::fwrite(p, sizeof(T), n, f);
+}
+}  // namespace
+
 extern "C" {
+
+// dataParsing (isar_imaging_export.cpp:48-66) through the reference's export
+// on the .wbd files in dir.  Writes to out_path: int32 [frame_len,
+// frame_num], dataN (double), turnAngle (float).
+int ref_parse(const char* dir, int polar_type, int data_type, const char* out_path)
+{
+    vec1D_DBL dn;
+    vec1D_FLT ta;
+    int frame_len = 0, frame_num = 0;
+    if (dataParsing(&dn, &ta, &frame_len, &frame_num, std::string(dir), polar_type, data_type) != 0) return -1;
+    FILE* f = std::fopen(out_path, "wb");
+    if (!f) return -2;
+    const int32_t fl[2] = {frame_len, frame_num};
+    dump(f, fl, 2);
+    dump(f, dn.data(), dn.size());
+    dump(f, ta.data(), ta.size());
+    std::fclose(f);
+    return 0;
+}
+
+// dataParsing, imagingMemInit and one dataExtracting
+// (isar_imaging_export.cpp:69-119) through the reference's exports: the
+// window of window_len pulses from window_head, every sampling_stride-th
+// pulse.  Writes to out_path: dataWFileSn (int32), dataNOut (double),
+// turnAngleOut (float), dataW (float I/Q pairs).
+int ref_extract(const char* dir, int polar_type, int data_type, int window_len, int window_head, int sampling_stride,
+                const char* out_path)
+{
+    vec1D_DBL dn;
+    vec1D_FLT ta;
+    int frame_len = 0, frame_num = 0;
+    if (dataParsing(&dn, &ta, &frame_len, &frame_num, std::string(dir), polar_type, data_type) != 0) return -1;
+    vec1D_FLT img;
+    vec1D_INT sn;
+    vec1D_DBL dn_out;
+    vec1D_FLT ta_out;
+    vec1D_COM_FLT dw;
+    imagingMemInit(&img, &sn, &dn_out, &ta_out, &dw, window_len, frame_len, data_type, true, false);
+    int imaging_stride = window_len;
+    const int rc = dataExtracting(&sn, &dn_out, &ta_out, &dw, dn, ta, frame_len, frame_num, sampling_stride,
+                                  window_head, window_len, imaging_stride, data_type);
+    int out = rc == 0 ? 0 : -3;
+    FILE* f = out == 0 ? std::fopen(out_path, "wb") : nullptr;
+    if (out == 0 && !f) out = -2;
+    if (f) {
+        dump(f, sn.data(), sn.size());
+        dump(f, dn_out.data(), dn_out.size());
+        dump(f, ta_out.data(), ta_out.size());
+        dump(f, reinterpret_cast<const float*>(dw.data()), 2 * dw.size());
+        std::fclose(f);
+    }
+    imagingMemDest(data_type, true, false);
+    return out;
+}
 
 // One frame through the reference.  echo: 2*M*N floats; velocity: M doubles.
 // img: M*512 floats (isarMainSingle).  Optional checkpoints recorded by a

@@ -9,7 +9,9 @@ parameters and the reference's outputs: the final image and the M x 512 cut
 after HRRPCenter + cutRangeProfile.  The pc_* fixtures hold seeded IFDS pulses
 (int16 I/Q, velocities, radar parameters) and the reference's pulse
 compression of each (its pulseCompression class, 4096 cells per pulse); the
-hrrp_* fixtures hold seeded int16 frames and the reference's getHRRP of them.
+hrrp_* fixtures hold seeded int16 frames and the reference's getHRRP of them;
+the ingest_* fixtures hold what the reference's dataParsing / dataExtracting
+return on the .wbd scenario of tests/wbd.py.
 
 Run here (where the reference checkout is present):
     python tests/golden/make_golden.py
@@ -27,13 +29,19 @@ os.environ.setdefault("ISAR_REFERENCE_DIR", "/root/reference/isar_imaging")
 
 import oracle  # noqa: E402
 from oracle import ref_emu  # noqa: E402
-from tests.helpers import CFG_FULL, CFG_PLAIN, PC_CASES, full_omega, make_ifds_pulses  # noqa: E402
+from tests.helpers import CFG_FULL, CFG_PLAIN, PC_CASES, full_omega, iq_checksum, make_ifds_pulses  # noqa: E402
 
 FIXTURES = {
     # name: (M, N, full pipeline (HPC + MTRC), seed)
     "plain_256x1024": (256, 1024, False, 101),
     "full_256x1024": (256, 1024, True, 102),
+    # the larger frames store their synthesis seed and a checksum of the
+    # int16 samples instead of the samples (tests regenerate them with the
+    # oracle's synthesis and check the checksum), and the image only
+    "full_512x4096": (512, 4096, True, 103),
+    "full_1024x8192": (1024, 8192, True, 41),
 }
+STORE_SAMPLES_UP_TO = 256 * 1024
 
 
 def make(name):
@@ -46,8 +54,12 @@ def make(name):
     echo = oracle.iq_to_c64(iq)
     out = ref_emu.frame(echo, vel, M, N, hpc=full, mtrc=full, checkpoints=True)
     path = os.path.join(HERE, name + ".npz")
-    np.savez_compressed(path, iq=iq, velocity=vel, M=M, N=N, B=1e9, fc=10e9, Fs=100e6, Tp=N / 100e6,
-                        hpc=full, mtrc=full, img=out["img"], cut=out["cut"])
+    common = dict(velocity=vel, M=M, N=N, B=1e9, fc=10e9, Fs=100e6, Tp=N / 100e6, hpc=full, mtrc=full,
+                  img=out["img"])
+    if M * N <= STORE_SAMPLES_UP_TO:
+        np.savez_compressed(path, iq=iq, cut=out["cut"], **common)
+    else:
+        np.savez_compressed(path, seed=seed, iq_checksum=iq_checksum(iq), **common)
     return path
 
 
@@ -84,6 +96,33 @@ def make_hrrp(name):
     return path
 
 
+INGEST_CASES = {
+    # name: (data_type, extract window (window_len, window_head, sampling_stride) or None)
+    "ingest_stretch": (2, (64, 30, 1)),
+    "ingest_ifds": (1, None),
+}
+
+
+def make_ingest(name):
+    """The reference's dataParsing (nav decode, turn-angle curve) and, for
+    STRETCH, one dataExtracting (uniform sampling, int16 samples to float)
+    on the .wbd scenario of tests/wbd.py (regenerated by the tests)."""
+    import tempfile
+    from tests.wbd import write_ingest_scenario
+    dt, win = INGEST_CASES[name]
+    with tempfile.TemporaryDirectory() as d:
+        write_ingest_scenario(d, data_type=dt)
+        fl, fn, dn, ta = ref_emu.parse(d, data_type=dt)
+        extra = {}
+        if win is not None:
+            sn, dno, tao, dw = ref_emu.extract(d, *win, data_type=dt)
+            extra = dict(window=np.array(win, np.int32), sn=sn, dataNOut=dno, turnAngleOut=tao, dataW=dw)
+    path = os.path.join(HERE, name + ".npz")
+    np.savez_compressed(path, data_type=dt, frame_len=fl, frame_num=fn, dataN=dn, turnAngle=ta, **extra)
+    return path
+
+
 if __name__ == "__main__":
-    for n in sys.argv[1:] or list(FIXTURES) + list(PC_CASES) + list(HRRP_CASES):
-        print(make_pc(n) if n in PC_CASES else make_hrrp(n) if n in HRRP_CASES else make(n))
+    for n in sys.argv[1:] or list(FIXTURES) + list(PC_CASES) + list(HRRP_CASES) + list(INGEST_CASES):
+        print(make_pc(n) if n in PC_CASES else make_hrrp(n) if n in HRRP_CASES else
+              make_ingest(n) if n in INGEST_CASES else make(n))

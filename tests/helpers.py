@@ -25,6 +25,29 @@ def make_frame(M, N, seed, full=False, **kw):
     return oracle.iq_to_c64(iq), vel
 
 
+def iq_checksum(iq):
+    """Order-sensitive checksum of int16 samples: (sum, sum of index * value)."""
+    a = np.asarray(iq, np.int64).ravel()
+    return np.array([a.sum(), (a * (np.arange(a.size, dtype=np.int64) % 65521)).sum()], np.int64)
+
+
+def golden_echo(z):
+    """The complex64 input of a golden fixture: its stored int16 samples, or,
+    for the larger fixtures, the frame regenerated from its seed by the
+    oracle's synthesis (checked against the stored checksum)."""
+    if "iq" in z:
+        return oracle.iq_to_c64(z["iq"])
+    M, N, seed, full = int(z["M"]), int(z["N"]), int(z["seed"]), bool(z["hpc"])
+    cfg = dict(CFG_FULL if full else CFG_PLAIN)
+    if full:
+        cfg["omega"] = full_omega(M)
+    cfg.update(M=M, N=N, seed=seed)
+    iq, vel = oracle.synth(cfg)
+    assert np.array_equal(iq_checksum(iq), z["iq_checksum"]), "synthesis differs from the fixture's"
+    assert np.array_equal(vel, z["velocity"])
+    return oracle.iq_to_c64(iq)
+
+
 def rel_l2(a, b):
     a = np.asarray(a, np.complex128)
     b = np.asarray(b, np.complex128)

@@ -45,3 +45,4 @@ def test_null_context_is_an_error():
     lib = g.load()
     assert lib.isar_image_host(None, None, None, 0, None) == -1
     assert lib.isar_destroy(None) == 0
+    assert lib.isar_test_barrier_timeout(None, 100, 1) == -1

@@ -6,7 +6,7 @@ import pytest
 
 import oracle
 from tests.helpers import make_frame, rel_l2
-from tests.test_gpu_parity import TOL_RA_FREE
+from tests.test_gpu_parity import TOL_IMG
 
 pytestmark = pytest.mark.gpu
 
@@ -57,7 +57,7 @@ def test_batch_equals_single_frame_and_oracle(torch_cuda, gb300):
             single = ctx.image_host(f["e"], f["v"], f["flags"])
         assert rel_l2(img, single) <= 1e-6, (f["M"], f["N"])
         want, _ = oracle.image(f["e"], f["v"], oracle.radar(f["M"], f["N"]), hpc=f["full"], mtrc=f["full"])
-        assert rel_l2(img, want) < TOL_RA_FREE, (f["M"], f["N"])
+        assert rel_l2(img, want) < TOL_IMG, (f["M"], f["N"])
 
 
 def test_batch_autotune_keeps_results(torch_cuda, gb300):
@@ -75,7 +75,7 @@ def test_batch_autotune_keeps_results(torch_cuda, gb300):
             assert t.af_cluster in (4, 8, 16) and t.ra_pair_min >= 1
     for f in fr:
         want, _ = oracle.image(f["e"], f["v"], oracle.radar(f["M"], f["N"]), hpc=f["full"], mtrc=f["full"])
-        assert rel_l2(f["img"].cpu().numpy(), want) < TOL_RA_FREE
+        assert rel_l2(f["img"].cpu().numpy(), want) < TOL_IMG
 
 
 def test_context_autotune_cooperative_or_cluster(torch_cuda, gb300):
@@ -88,7 +88,7 @@ def test_context_autotune_cooperative_or_cluster(torch_cuda, gb300):
         t = ctx.autotune(de, None, 0, engines=3)
         assert t.af_cluster in (0, 4, 8, 16)
         got = ctx.image_host(e, v, 0)
-    assert rel_l2(got, want) < TOL_RA_FREE
+    assert rel_l2(got, want) < TOL_IMG
 
 
 def test_misaligned_echo_is_rejected_before_any_launch(torch_cuda, gb300):
