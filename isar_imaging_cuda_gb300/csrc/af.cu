@@ -482,21 +482,24 @@ struct AFFrame {
     const int* bins;       // [U]
     const int* fdec;       // [1] = U
     float2* phase;         // [M] in: Doppler-tracking start phase, out: final phase
-    int* stat;             // [0] iterations applied (both legs), [1] final entropy bits,
-                           // [2] learned leg kept, [3], [4] final entropy bits of the
-                           // Doppler and learned legs, [5], [6] their iterations;
-                           // may be null
+    int* stat;             // [0] iterations applied (both legs), [1] entropy bits of the
+                           // selected bins at the last evaluated phase, [2] learned leg
+                           // kept (set by the image judge), [3], [4] those entropy bits
+                           // of the plain and the learned leg, [5], [6] their
+                           // iterations; may be null
     float2* alt;           // [M] learned start phase in, the learned leg's final phase
                            // out (warm start), or null
     float2* gcol;          // [U][M] scratch: contiguous copy of the bin columns
 };
 
 // With a learned start (AFFrame::alt), both cluster engines run two legs: the
-// autofocus from the learned start until the stop criterion, then from the
-// Doppler-tracking start until the same criterion (the plain autofocus), and
-// keep the final phase whose entropy of the selected bins is lower.  The
-// autofocus is the judge: a frame on which the learned start ends worse
-// reverts to the plain result.
+// autofocus from the learned start until the stop criterion (`tol`), then the
+// plain autofocus, the reference's algorithm (Doppler-tracking start, `iters`
+// updates, no stop criterion).  Both final phases are returned (alt, phase);
+// the judge downstream images both and keeps the lower final image entropy,
+// so a frame on which the learned start ends worse reverts to the plain
+// result.  (The entropy of the selected bins cannot judge: it ignores a
+// linear phase, a Doppler shift of the image, which MTRC does not.)
 
 template <int M>
 __global__ void __launch_bounds__(AFC<M>::THREADS, 1)
@@ -642,7 +645,7 @@ k_af_cluster(AFFrame f, int iters, float tol, const float2* __restrict__ tw)
     // when the stop criterion ends it.  Returns (in thread 0) the entropy at
     // the last evaluated phase or, with want_final, of the final phase (one
     // more entropy sweep when all `iters` updates were applied).
-    auto leg = [&](bool want_final, int& used) -> float {
+    auto leg = [&](bool want_final, float ltol, int& used) -> float {
         float e_prev = 0.0f, e_last = 0.0f;   // meaningful in thread 0
         bool stopped = false;
         used = iters;
@@ -650,7 +653,7 @@ k_af_cluster(AFFrame f, int iters, float tol, const float2* __restrict__ tw)
         for (int it = 0; it < iters; ++it) {
             // the entropy is needed by the stop criterion, and for the trace at
             // the last iteration; elsewhere its logarithms are skipped
-            const bool check = tol > 0.0f && it % kStopEvery == 0;
+            const bool check = ltol > 0.0f && it % kStopEvery == 0;
             const bool need_e = check || it == iters - 1;
             float s1 = 0.0f, s2 = 0.0f;
             sweep(true, need_e, s1, s2);
@@ -659,7 +662,7 @@ k_af_cluster(AFFrame f, int iters, float tol, const float2* __restrict__ tw)
                 bool stop = false;
                 if (need_e) {
                     if (check) {
-                        stop = it > 0 && fabsf(E - e_prev) <= (float)kStopEvery * tol * fabsf(E);
+                        stop = it > 0 && fabsf(E - e_prev) <= (float)kStopEvery * ltol * fabsf(E);
                         e_prev = E;
                     }
                     e_last = E;
@@ -711,7 +714,7 @@ k_af_cluster(AFFrame f, int iters, float tol, const float2* __restrict__ tw)
 
     if (!f.alt) {
         int used;
-        const float e = leg(false, used);
+        const float e = leg(false, tol, used);
         for (int m = r * rows + tid; m < (r + 1) * rows; m += A::THREADS) f.phase[m] = ph[m];
         if (r == 0 && tid == 0 && f.stat) {
             f.stat[0] = used;
@@ -719,26 +722,22 @@ k_af_cluster(AFFrame f, int iters, float tol, const float2* __restrict__ tw)
         }
         return;
     }
-    // learned leg, then the plain leg from the Doppler-tracking start; the
-    // lower final entropy is kept
+    // the learned leg, then the plain leg (see AFFrame)
     __syncthreads();
     for (int m = tid; m < M; m += A::THREADS) ph[m] = f.alt[m];
     __syncthreads();
     int used_l, used_d;
-    const float e_l = leg(true, used_l);
+    const float e_l = leg(false, tol, used_l);
     for (int m = r * rows + tid; m < (r + 1) * rows; m += A::THREADS) f.alt[m] = ph[m];
     __syncthreads();
     for (int m = tid; m < M; m += A::THREADS) ph[m] = f.phase[m];
     __syncthreads();
-    const float e_d = leg(true, used_d);
-    if (tid == 0) red[43] = e_l < e_d ? 1.0 : 0.0;
-    __syncthreads();
-    const bool keep_l = red[43] != 0.0;
-    for (int m = r * rows + tid; m < (r + 1) * rows; m += A::THREADS) f.phase[m] = keep_l ? f.alt[m] : ph[m];
+    const float e_d = leg(false, 0.0f, used_d);
+    for (int m = r * rows + tid; m < (r + 1) * rows; m += A::THREADS) f.phase[m] = ph[m];
     if (r == 0 && tid == 0 && f.stat) {
         f.stat[0] = used_l + used_d;
-        f.stat[1] = __float_as_int(keep_l ? e_l : e_d);
-        f.stat[2] = keep_l ? 1 : 0;
+        f.stat[1] = __float_as_int(e_d);
+        f.stat[2] = 0;
         f.stat[3] = __float_as_int(e_d);
         f.stat[4] = __float_as_int(e_l);
         f.stat[5] = used_d;
@@ -933,7 +932,7 @@ k_af_cluster_w1024(AFFrame f, int iters, float tol, const float2* __restrict__ t
     // warp 0, the entropy at the last evaluated phase or, with want_final, of
     // the final phase.
     float2* buf = tiles + AFW::TILE;   // behind P (tile 0 holds P)
-    auto leg = [&](bool want_final, int& used) -> float {
+    auto leg = [&](bool want_final, float ltol, int& used) -> float {
         float e_prev = 0.0f, e_last = 0.0f;   // meaningful in warp 0
         bool stopped = false;
         used = iters;
@@ -942,7 +941,7 @@ k_af_cluster_w1024(AFFrame f, int iters, float tol, const float2* __restrict__ t
 #pragma unroll 1
         for (int it = 0; it < iters; ++it) {
             // the entropy is needed by the stop criterion or for the last trace
-            const bool check = tol > 0.0f && it % kStopEvery == 0;
+            const bool check = ltol > 0.0f && it % kStopEvery == 0;
             const bool need_e = check || it == iters - 1;
             float s1 = 0.0f, s2 = 0.0f;
             sweep(true, need_e, s1, s2);
@@ -953,7 +952,7 @@ k_af_cluster_w1024(AFFrame f, int iters, float tol, const float2* __restrict__ t
                 if (need_e) {
                     const float E = entropy_total();
                     if (check) {
-                        stop = it > 0 && fabsf(E - e_prev) <= (float)kStopEvery * tol * fabsf(E);
+                        stop = it > 0 && fabsf(E - e_prev) <= (float)kStopEvery * ltol * fabsf(E);
                         e_prev = E;
                     }
                     e_last = E;
@@ -1008,7 +1007,7 @@ k_af_cluster_w1024(AFFrame f, int iters, float tol, const float2* __restrict__ t
 
     if (!f.alt) {
         int used;
-        const float e = leg(false, used);
+        const float e = leg(false, tol, used);
         for (int m = r * rows + tid; m < (r + 1) * rows; m += AFW::THREADS) f.phase[m] = ph[m];
         if (r == 0 && tid == 0 && f.stat) {
             f.stat[0] = used;
@@ -1016,26 +1015,22 @@ k_af_cluster_w1024(AFFrame f, int iters, float tol, const float2* __restrict__ t
         }
         return;
     }
-    // learned leg, then the plain leg from the Doppler-tracking start; the
-    // lower final entropy is kept (see AFFrame)
+    // the learned leg, then the plain leg (see AFFrame)
     __syncthreads();
     for (int m = tid; m < M; m += AFW::THREADS) ph[m] = f.alt[m];
     __syncthreads();
     int used_l, used_d;
-    const float e_l = leg(true, used_l);
+    const float e_l = leg(false, tol, used_l);
     for (int m = r * rows + tid; m < (r + 1) * rows; m += AFW::THREADS) f.alt[m] = ph[m];
     __syncthreads();
     for (int m = tid; m < M; m += AFW::THREADS) ph[m] = f.phase[m];
     __syncthreads();
-    const float e_d = leg(true, used_d);
-    if (tid == 0) red[43] = e_l < e_d ? 1.0 : 0.0;
-    __syncthreads();
-    const bool keep_l = red[43] != 0.0;
-    for (int m = r * rows + tid; m < (r + 1) * rows; m += AFW::THREADS) f.phase[m] = keep_l ? f.alt[m] : ph[m];
+    const float e_d = leg(false, 0.0f, used_d);
+    for (int m = r * rows + tid; m < (r + 1) * rows; m += AFW::THREADS) f.phase[m] = ph[m];
     if (r == 0 && tid == 0 && f.stat) {
         f.stat[0] = used_l + used_d;
-        f.stat[1] = __float_as_int(keep_l ? e_l : e_d);
-        f.stat[2] = keep_l ? 1 : 0;
+        f.stat[1] = __float_as_int(e_d);
+        f.stat[2] = 0;
         f.stat[3] = __float_as_int(e_d);
         f.stat[4] = __float_as_int(e_l);
         f.stat[5] = used_d;
@@ -1049,6 +1044,20 @@ __global__ void k_af_apply(float2* __restrict__ cut, const float2* __restrict__ 
     const int m = blockIdx.x;
     const float2 p = phase[m];
     for (int c = threadIdx.x; c < C; c += blockDim.x) cut[(size_t)m * C + c] = cmul(p, cut[(size_t)m * C + c]);
+}
+
+// Both legs of a warm-started frame in one pass: cut2 = diag(phase_l) cut
+// (the learned leg), then cut = diag(phase) cut in place (the plain leg).
+__global__ void k_af_apply2(float2* __restrict__ cut, const float2* __restrict__ phase,
+                            const float2* __restrict__ phase_l, float2* __restrict__ cut2, int M)
+{
+    const int m = blockIdx.x;
+    const float2 p = phase[m], pl = phase_l[m];
+    for (int c = threadIdx.x; c < C; c += blockDim.x) {
+        const float2 x = cut[(size_t)m * C + c];
+        cut2[(size_t)m * C + c] = cmul(pl, x);
+        cut[(size_t)m * C + c] = cmul(p, x);
+    }
 }
 
 // ---------------------------------------------------------------------------
@@ -1226,7 +1235,10 @@ static cudaError_t fe_run_m(const FEArgs& a, cudaStream_t st)
             return e;
         ISAR_COUNT(1);
     }
-    k_af_apply<<<M, 256, 0, st>>>(a.cut, a.phase, M);
+    if (a.ws_w && a.iters > 0 && a.af_cluster > 0)
+        k_af_apply2<<<M, 256, 0, st>>>(a.cut, a.phase, a.ws_phase, a.cut2, M);
+    else
+        k_af_apply<<<M, 256, 0, st>>>(a.cut, a.phase, M);
     ISAR_COUNT(1);
     return cudaGetLastError();
 }

@@ -201,6 +201,9 @@ struct isar_ctx {
     isar::nn::Acts ws_a;
     float* d_ws_psi = nullptr;
     float2* d_ws_phase = nullptr;
+    float2* d_cut2 = nullptr;      // the learned leg's cut, image and judge scratch
+    float* d_img2 = nullptr;
+    double* d_judge = nullptr;
     int* d_ws_err = nullptr;
     bool ws_alloc = false;
 };
@@ -396,6 +399,7 @@ isar::FEArgs fe_args(isar_ctx* c, float2* cut, int iters)
         a.ws_psi = c->d_ws_psi;
         a.ws_phase = c->d_ws_phase;
         a.ws_err = c->d_ws_err;
+        a.cut2 = c->d_cut2;
     }
     return a;
 }
@@ -458,6 +462,12 @@ int run_frame_eager(isar_ctx* c, const float2* x, const double* d_vel, int flags
     CU(isar::center_cut(c->d_arp, c->d_x, c->M, c->N, c->d_dec, c->d_cut, c->st));
     CU(isar::fe_run(fe_args(c, c->d_cut, c->af_iters), c->st));
     CU(isar::post_run(post_args(c, c->d_cut, flags, d_img), c->st));
+    if (c->ws_w && c->af_iters > 0) {
+        // warm start: image the learned leg too; the judge keeps the lower
+        // final image entropy in d_img
+        CU(isar::post_run(post_args(c, c->d_cut2, flags, c->d_img2), c->st));
+        CU(isar::img_judge(d_img, c->d_img2, c->M * kRangeCut, c->d_judge, c->d_fdec + 4, c->st));
+    }
     return ISAR_OK;
 }
 
@@ -769,6 +779,9 @@ ISAR_API int isar_set_warmstart(isar_ctx* c, const isar_wsnet* net)
         TRY(dalloc(c, &c->d_ws_psi, M));
         TRY(dalloc(c, &c->d_ws_phase, M));
         TRY(dalloc(c, &c->d_ws_err, 1));
+        TRY(dalloc(c, &c->d_cut2, M * kRangeCut));
+        TRY(dalloc(c, &c->d_img2, M * kRangeCut));
+        TRY(dalloc(c, &c->d_judge, (size_t)isar::kJudgeParts * 4));
         CU(cudaMemsetAsync(c->d_ws_err, 0, sizeof(int), c->st));
         c->ws_alloc = true;
     }
@@ -876,7 +889,11 @@ ISAR_API int isar_stage_fast_entropy(isar_ctx* c, float* d_cut, int iterations)
 {
     TRY(check_ctx(c));
     if (!d_cut || iterations < 0) return fail(ISAR_EINVAL, "bad argument");
-    CU(isar::fe_run(fe_args(c, reinterpret_cast<float2*>(d_cut), iterations), c->st));
+    // the stage alone runs the plain autofocus: a warm start is judged on
+    // final images, which only the whole frame produces
+    isar::FEArgs a = fe_args(c, reinterpret_cast<float2*>(d_cut), iterations);
+    a.ws_w = nullptr;
+    CU(isar::fe_run(a, c->st));
     return ISAR_OK;
 }
 

@@ -123,7 +123,8 @@ struct FEArgs {
     const nn::Weights* ws_w;
     nn::Acts* ws_a;          // inference activations for M rows; act[0] receives the features
     float* ws_psi;           // [M]
-    float2* ws_phase;        // [M] warm-start phase
+    float2* ws_phase;        // [M] warm-start phase in, the learned leg's final phase out
+    float2* cut2;            // [M][512] the learned leg's phase applied to the cut (warm start)
     int* ws_err;             // GEMM wait-timeout flag
     int pre_only;            // stop after the bin selection and the Doppler start phase
 };
@@ -131,6 +132,14 @@ struct FEArgs {
 // Largest cluster the device accepts for the autofocus engine with M pulses
 // (16, 8, 4, or 0 when clusters cannot be launched).
 int af_cluster_max(int M);
+
+// The judge of a warm-started frame: the final image entropies of img (the
+// plain leg) and img_l (the learned leg), M*512 floats each; img_l is copied
+// over img when its entropy is lower, and stat[2] (the autofocus statistics)
+// records the choice, stat[1] the kept leg's entropy of the selected bins.
+// part: kJudgeParts * 4 doubles of scratch.
+constexpr int kJudgeParts = 64;
+cudaError_t img_judge(float* img, const float* img_l, int n, double* part, int* stat, cudaStream_t st);
 
 struct PostArgs {
     int M;

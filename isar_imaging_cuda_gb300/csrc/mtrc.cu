@@ -212,4 +212,81 @@ cudaError_t post_run(const PostArgs& a, cudaStream_t st)
     }
 }
 
+// ---------------------------------------------------------------------------
+// Judge of a warm-started frame.  Final image entropy (the project's
+// definition, as the bench measures it): E = -sum p ln p with p = I^2 / S,
+// S = sum I^2, i.e. E = ln S - T / S with T = sum I^2 ln I^2.  Float terms,
+// double accumulation; CTA b of image i (blockIdx.y) writes (S, T) partials
+// to part[(i * kJudgeParts + b) * 2].
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ double block_sum_d(double v, double* red)
+{
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    __syncthreads();
+    if (lane == 0) red[w] = v;
+    __syncthreads();
+    double s = 0.0;
+    if (threadIdx.x == 0)
+        for (int i = 0; i < (int)(blockDim.x >> 5); ++i) s += red[i];   // fixed order
+    return s;
+}
+
+__global__ void __launch_bounds__(256) k_img_entropy_part(const float* __restrict__ img, const float* __restrict__ img_l,
+                                                          int n, double* __restrict__ part)
+{
+    __shared__ double red[8];
+    const float* x = blockIdx.y ? img_l : img;
+    double s = 0.0, t = 0.0;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const float v = x[i];
+        const float p = v * v;
+        s += (double)p;
+        if (p > 0.0f) t += (double)(p * logf(p));
+    }
+    s = block_sum_d(s, red);
+    t = block_sum_d(t, red);
+    if (threadIdx.x == 0) {
+        double* q = part + ((size_t)blockIdx.y * gridDim.x + blockIdx.x) * 2;
+        q[0] = s;
+        q[1] = t;
+    }
+}
+
+// Every CTA forms both entropies from the partials in the same order (same
+// decision everywhere) and copies its slice of img_l over img when the
+// learned leg's entropy is lower; NaN keeps the plain leg.
+__global__ void __launch_bounds__(256) k_img_select(float* __restrict__ img, const float* __restrict__ img_l, int n,
+                                                    const double* __restrict__ part, int* stat)
+{
+    __shared__ int s_keep;
+    if (threadIdx.x == 0) {
+        double S[2] = {0.0, 0.0}, T[2] = {0.0, 0.0};
+        for (int i = 0; i < 2; ++i)
+            for (int b = 0; b < kJudgeParts; ++b) {
+                S[i] += part[(i * kJudgeParts + b) * 2];
+                T[i] += part[(i * kJudgeParts + b) * 2 + 1];
+            }
+        const double e = log(S[0]) - T[0] / S[0], el = log(S[1]) - T[1] / S[1];
+        s_keep = el < e ? 1 : 0;
+        if (blockIdx.x == 0 && stat) {
+            stat[2] = s_keep;
+            if (s_keep) stat[1] = stat[4];
+        }
+    }
+    __syncthreads();
+    if (!s_keep) return;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) img[i] = img_l[i];
+}
+
+cudaError_t img_judge(float* img, const float* img_l, int n, double* part, int* stat, cudaStream_t st)
+{
+    k_img_entropy_part<<<dim3(kJudgeParts, 2), 256, 0, st>>>(img, img_l, n, part);
+    ISAR_COUNT(1);
+    k_img_select<<<kJudgeParts, 256, 0, st>>>(img, img_l, n, part, stat);
+    ISAR_COUNT(1);
+    return cudaGetLastError();
+}
+
 }  // namespace isar

@@ -158,10 +158,10 @@ def image_entropy(img):
 
 def evaluate_autofocus(torch, params, kind, n, tol=1e-6, cluster=16, seed0=EVAL_SEED0):
     """Per frame: the reference's autofocus (Doppler-tracking start, 120
-    iterations) and the judged warm start (the learned leg and the plain leg,
-    each until the stop criterion `tol`, the lower final entropy of the
-    selected bins kept).  Returns per-frame iterations of both legs, their
-    final entropies of the selected bins, which leg was kept and the final
+    iterations) and the judged warm start (the learned leg until the stop
+    criterion `tol`, the plain leg = the reference's autofocus, the lower
+    final image entropy kept).  Returns per frame the iterations of both legs,
+    their entropies of the selected bins, which leg was kept and the final
     image entropies."""
     w = workload(kind)
     M, N = w["M"], w["N"]
@@ -198,22 +198,20 @@ def evaluate_autofocus(torch, params, kind, n, tol=1e-6, cluster=16, seed0=EVAL_
 
 
 def summarize(rows):
-    """Iterations of the plain and learned legs, how often the learned leg
-    was kept, and the judged result's final image entropy against the
-    reference's 120 iterations."""
+    """Iterations of the learned leg (to the stop criterion) and of the plain
+    leg (the reference's fixed count), how often the learned leg was kept,
+    and the judged final image entropy against the reference's autofocus
+    (negative: the network's gain)."""
     e120 = np.array([r["ref120"]["entropy"] for r in rows])
     ej = np.array([r["judged"]["entropy"] for r in rows])
+    kept = np.array([r["judged"]["ws_used"] for r in rows], bool)
     it_p = np.array([r["judged"]["legs_iters"][0] for r in rows], float)
     it_l = np.array([r["judged"]["legs_iters"][1] for r in rows], float)
-    en_p = np.array([r["judged"]["legs_entropy"][0] for r in rows], float)
-    en_l = np.array([r["judged"]["legs_entropy"][1] for r in rows], float)
+    d = ej - e120
     return dict(frames=len(rows), iters_plain_leg=float(it_p.mean()), iters_learned_leg=float(it_l.mean()),
-                iters_saved_frac=float(1.0 - it_l.mean() / it_p.mean()),
-                learned_kept_frac=float(np.mean([r["judged"]["ws_used"] for r in rows])),
-                bins_entropy_gain_mean=float(np.mean(en_p - en_l)),
-                learned_leg_not_worse_frac=float(np.mean(en_l <= en_p + 1e-4 * np.abs(en_p))),
-                dE_judged_vs_ref120_max=float(np.max(ej - e120)),
-                dE_judged_vs_ref120_mean=float(np.mean(ej - e120)))
+                learned_kept_frac=float(kept.mean()),
+                dE_judged_vs_ref120_max=float(d.max()), dE_judged_vs_ref120_mean=float(d.mean()),
+                dE_kept_frames_mean=float(d[kept].mean()) if kept.any() else 0.0)
 
 
 def main():

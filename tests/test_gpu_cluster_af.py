@@ -4,7 +4,7 @@ import numpy as np
 import pytest
 
 import oracle
-from tests.helpers import make_frame, rel_l2
+from tests.helpers import golden_echo, make_frame, rel_l2
 from tests.test_gpu_parity import TOL_IMG, ctx_for, from_dev, to_dev
 
 pytestmark = pytest.mark.gpu
@@ -89,12 +89,12 @@ def test_cluster_engine_whole_frame_matches_reference_golden(torch_cuda, gb300):
     import os
     torch = torch_cuda
     for path in sorted(glob.glob(os.path.join(os.path.dirname(__file__), "golden", "*.npz"))):
-        if os.path.basename(path).startswith(("pc_", "hrrp_")):   # stage fixtures, not frames
+        if os.path.basename(path).startswith(("pc_", "hrrp_", "ingest_")):   # stage fixtures, not frames
             continue
         z = np.load(path)
         M, N = int(z["M"]), int(z["N"])
         flags = (gb300.FLAG_HPC if bool(z["hpc"]) else 0) | (gb300.FLAG_MTRC if bool(z["mtrc"]) else 0)
-        echo = oracle.iq_to_c64(z["iq"])
+        echo = golden_echo(z)
         rp = oracle.radar(M, N, B=float(z["B"]), fc=float(z["fc"]), Fs=float(z["Fs"]), Tp=float(z["Tp"]))
         _, tw = oracle.image(echo, z["velocity"], rp, hpc=bool(z["hpc"]), mtrc=bool(z["mtrc"]))
         with ctx_for(gb300, torch, M, N) as ctx:
