@@ -9,10 +9,11 @@ distinct frames imaged by one CUDA graph (isar_batch_run: per-shape lanes,
 cluster-resident autofocus), inputs resident in HBM (8 GiB > L2).  Three
 autofocus arms are tried in order and the first whose images pass the
 equal-entropy check is timed: (1) the learned warm start judged by the plain
-autofocus (the autofocus runs from the network's start and from the
-Doppler-tracking start, each until the entropy stop criterion, and keeps the
-lower final entropy), (2) the stop criterion alone (Doppler-tracking start),
-(3) the reference algorithm (120 iterations).  The check, per frame: no
+autofocus (the autofocus runs from the network's start until the entropy stop
+criterion and, as the reference does, from the Doppler-tracking start for 120
+iterations; both are imaged and the lower final image entropy is kept), (2)
+the stop criterion alone (Doppler-tracking start), (3) the reference
+algorithm (120 iterations).  The check, per frame: no
 frame's final image entropy may exceed the plain pipeline's on the same frame
 by more than 1e-4.  Every arm's check is reported.
 `plain` is the single-frame pipeline (isar_image_device, the reference's
@@ -43,9 +44,11 @@ M, N = 1024, 8192
 C = 512
 B = 128                     # frames per batch step
 TOL = 3e-7                  # autofocus entropy stop criterion (relative change per iteration)
+TOL_LEARNED = 3e-6          # the learned leg's stop criterion (its gain is the same as at 3e-7, 26% fewer iterations)
 E2E_SETS = 3                # end-to-end buffer sets in rotation (copies of later steps run ahead)
 METRIC = "frames/s @1024×8192 c64: learned+batched vs plain on 1 GB300, equal entropy"
-ARMS = [("learned warm start judged by the plain autofocus (both to the entropy stop criterion)", True, TOL),
+ARMS = [("learned warm start (to the entropy stop criterion) judged against the plain autofocus (120 iterations) "
+         "on final image entropy", True, TOL_LEARNED),
         ("entropy stop criterion, Doppler-tracking start", False, TOL),
         ("reference algorithm (120 iterations)", False, 0.0)]
 WORKLOAD = ("full five-stage pipeline, 1024 pulses x 8192 range cells complex64, HPC + MTRC on, "
@@ -582,7 +585,7 @@ def run_profile(args):
             if learned:
                 b.set_warmstart(net)
             b.set_tuning(rp, g.Tuning(ra_pair_min=128, ra_rows_per_cta=16, ra_rows_final=16, af_cluster=8,
-                                      af_tol=TOL if learned else 0.0, af_iters=120, af_cluster_max=0))
+                                      af_tol=TOL_LEARNED if learned else 0.0, af_iters=120, af_cluster_max=0))
             lst = g.Batch.frames((rp, X[i], V[i], flags, imgs[i]) for i in range(nb))
             for _ in range(args.warmup + args.steps):
                 b.run(lst)

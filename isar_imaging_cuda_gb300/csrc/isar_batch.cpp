@@ -536,7 +536,7 @@ ISAR_API int isar_batch_autotune(isar_batch* b, const isar_batch_frame* f, int n
     int best_l = b->lanes, best_cl = 0;
     for (int cl : {16, 8}) {
         TRY(apply(set_cluster(cl)));
-        for (int L : {1, 2, 4, 8, 16, 32}) {
+        for (int L : {1, 2, 4, 8, 16, 32, 64}) {
             if (L > 1 && L / 2 >= most) break;
             float ms = 0.0f;
             TRY(time_with(L, &ms));
