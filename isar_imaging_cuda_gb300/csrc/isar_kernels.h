@@ -117,8 +117,10 @@ struct FEArgs {
     // the 4 iterations between two checks); 0 runs all `iters` (the
     // reference's fixed count).
     float tol;
-    int* af_stat;            // [0] iterations applied, [1] entropy (float bits), [2] warm start used,
-                             // [3], [4] start entropies (float bits); may be null
+    int* af_stat;            // [0] iterations applied (both legs with a warm start), [1] entropy
+                             // (float bits), [2] learned leg kept (set by the image judge),
+                             // [3], [4] entropies of the plain and learned legs (float bits),
+                             // [5], [6] their iterations; may be null
     // Learned warm start (cluster engine only), or ws_w == nullptr.
     const nn::Weights* ws_w;
     nn::Acts* ws_a;          // inference activations for M rows; act[0] receives the features
@@ -138,7 +140,8 @@ int af_cluster_max(int M);
 // over img when its entropy is lower, and stat[2] (the autofocus statistics)
 // records the choice, stat[1] the kept leg's entropy of the selected bins.
 // part: kJudgeParts * 4 doubles of scratch.
-constexpr int kJudgeParts = 64;
+constexpr int kJudgeParts = 256;   // CTAs per image of the entropy sums
+constexpr int kJudgeCopy = 128;    // CTAs of the decision and copy
 cudaError_t img_judge(float* img, const float* img_l, int n, double* part, int* stat, cudaStream_t st);
 
 struct PostArgs {

@@ -215,64 +215,76 @@ cudaError_t post_run(const PostArgs& a, cudaStream_t st)
 // ---------------------------------------------------------------------------
 // Judge of a warm-started frame.  Final image entropy (the project's
 // definition, as the bench measures it): E = -sum p ln p with p = I^2 / S,
-// S = sum I^2, i.e. E = ln S - T / S with T = sum I^2 ln I^2.  Float terms,
-// double accumulation; CTA b of image i (blockIdx.y) writes (S, T) partials
-// to part[(i * kJudgeParts + b) * 2].
+// S = sum I^2, i.e. E = ln S - ln 2 * T / S with T = sum I^2 log2 I^2 (the
+// hardware base-2 logarithm).  Float sums per thread, double across warps
+// and CTAs; CTA b of image i (blockIdx.y) writes its (S, T) partials to
+// part[(i * kJudgeParts + b) * 2].
 // ---------------------------------------------------------------------------
-__device__ __forceinline__ double block_sum_d(double v, double* red)
-{
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    __syncthreads();
-    if (lane == 0) red[w] = v;
-    __syncthreads();
-    double s = 0.0;
-    if (threadIdx.x == 0)
-        for (int i = 0; i < (int)(blockDim.x >> 5); ++i) s += red[i];   // fixed order
-    return s;
-}
-
 __global__ void __launch_bounds__(256) k_img_entropy_part(const float* __restrict__ img, const float* __restrict__ img_l,
                                                           int n, double* __restrict__ part)
 {
-    __shared__ double red[8];
+    __shared__ double red[2][8];
     const float* x = blockIdx.y ? img_l : img;
-    double s = 0.0, t = 0.0;
+    float s = 0.0f, t = 0.0f;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         const float v = x[i];
         const float p = v * v;
-        s += (double)p;
-        if (p > 0.0f) t += (double)(p * logf(p));
+        s += p;
+        if (p > 0.0f) t += p * __log2f(p);
     }
-    s = block_sum_d(s, red);
-    t = block_sum_d(t, red);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        s += __shfl_xor_sync(0xffffffffu, s, o);
+        t += __shfl_xor_sync(0xffffffffu, t, o);
+    }
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    if (lane == 0) {
+        red[0][w] = s;
+        red[1][w] = t;
+    }
+    __syncthreads();
     if (threadIdx.x == 0) {
+        double S = 0.0, T = 0.0;
+        for (int i = 0; i < (int)(blockDim.x >> 5); ++i) {   // fixed order
+            S += red[0][i];
+            T += red[1][i];
+        }
         double* q = part + ((size_t)blockIdx.y * gridDim.x + blockIdx.x) * 2;
-        q[0] = s;
-        q[1] = t;
+        q[0] = S;
+        q[1] = T;
     }
 }
 
-// Every CTA forms both entropies from the partials in the same order (same
-// decision everywhere) and copies its slice of img_l over img when the
-// learned leg's entropy is lower; NaN keeps the plain leg.
+// Every CTA forms both entropies from the partials in the same order (warp 0:
+// a lane per partial slice, then a fixed xor tree, so every CTA takes the
+// same decision) and copies its slice of img_l over img when the learned
+// leg's entropy is lower; NaN keeps the plain leg.
 __global__ void __launch_bounds__(256) k_img_select(float* __restrict__ img, const float* __restrict__ img_l, int n,
                                                     const double* __restrict__ part, int* stat)
 {
     __shared__ int s_keep;
-    if (threadIdx.x == 0) {
-        double S[2] = {0.0, 0.0}, T[2] = {0.0, 0.0};
-        for (int i = 0; i < 2; ++i)
-            for (int b = 0; b < kJudgeParts; ++b) {
-                S[i] += part[(i * kJudgeParts + b) * 2];
-                T[i] += part[(i * kJudgeParts + b) * 2 + 1];
+    if (threadIdx.x < 32) {
+        const int lane = threadIdx.x;
+        double v[4] = {0.0, 0.0, 0.0, 0.0};   // S, T of the plain leg, S, T of the learned leg
+        for (int b = lane; b < kJudgeParts; b += 32)
+#pragma unroll
+            for (int i = 0; i < 2; ++i) {
+                v[2 * i] += part[(i * kJudgeParts + b) * 2];
+                v[2 * i + 1] += part[(i * kJudgeParts + b) * 2 + 1];
             }
-        const double e = log(S[0]) - T[0] / S[0], el = log(S[1]) - T[1] / S[1];
-        s_keep = el < e ? 1 : 0;
-        if (blockIdx.x == 0 && stat) {
-            stat[2] = s_keep;
-            if (s_keep) stat[1] = stat[4];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1)
+#pragma unroll
+            for (int k = 0; k < 4; ++k) v[k] += __shfl_xor_sync(0xffffffffu, v[k], o);
+        if (lane == 0) {
+            const float ln2 = 0.693147180559945309f;
+            const float e = logf((float)v[0]) - ln2 * (float)(v[1] / v[0]);
+            const float el = logf((float)v[2]) - ln2 * (float)(v[3] / v[2]);
+            s_keep = el < e ? 1 : 0;
+            if (blockIdx.x == 0 && stat) {
+                stat[2] = s_keep;
+                if (s_keep) stat[1] = stat[4];
+            }
         }
     }
     __syncthreads();
@@ -284,7 +296,7 @@ cudaError_t img_judge(float* img, const float* img_l, int n, double* part, int* 
 {
     k_img_entropy_part<<<dim3(kJudgeParts, 2), 256, 0, st>>>(img, img_l, n, part);
     ISAR_COUNT(1);
-    k_img_select<<<kJudgeParts, 256, 0, st>>>(img, img_l, n, part, stat);
+    k_img_select<<<kJudgeCopy, 256, 0, st>>>(img, img_l, n, part, stat);
     ISAR_COUNT(1);
     return cudaGetLastError();
 }

@@ -269,16 +269,35 @@ k_features(const float2* __restrict__ cut, const double* __restrict__ E, const f
         }
         __syncthreads();
     }
-    // per-bin mean magnitudes of the pulse-pair products
+    // per-bin mean magnitudes of the pulse-pair products: per-thread sums in
+    // registers, then a fixed-order block reduction (deterministic, no
+    // shared-memory atomics)
+    float acc[kFeatBins + 1];
+#pragma unroll
+    for (int q = 0; q <= kFeatBins; ++q) acc[q] = 0.0f;
     for (int m = tid; m < M - 1; m += blockDim.x) {
-#pragma unroll 4
+#pragma unroll
         for (int q = 0; q < kFeatBins; ++q) {
             const int b = s_bins[q];
             const float2 p = cmulc(cut[(size_t)m * C + b], cut[(size_t)(m + 1) * C + b]);
-            atomicAdd(&s_sum[q], sqrtf(p.x * p.x + p.y * p.y));
+            acc[q] += sqrtf(p.x * p.x + p.y * p.y);
         }
         const float2 d = dsum[m];
-        atomicAdd(&s_sum[kFeatBins], sqrtf(d.x * d.x + d.y * d.y));
+        acc[kFeatBins] += sqrtf(d.x * d.x + d.y * d.y);
+    }
+    __shared__ float s_part[kFeatBins + 1][8];
+#pragma unroll
+    for (int q = 0; q <= kFeatBins; ++q) {
+        float v = acc[q];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+        if (lane == 0) s_part[q][w] = v;
+    }
+    __syncthreads();
+    if (tid <= kFeatBins) {
+        float v = 0.0f;
+        for (int i = 0; i < (int)(blockDim.x >> 5); ++i) v += s_part[tid][i];
+        s_sum[tid] = v;
     }
     __syncthreads();
     for (int m = tid; m < M; m += blockDim.x) {

