@@ -98,7 +98,7 @@ def make_hrrp(name):
 
 INGEST_CASES = {
     # name: (data_type, extract window (window_len, window_head, sampling_stride) or None)
-    "ingest_stretch": (2, (64, 30, 1)),
+    "ingest_stretch": (2, (128, 30, 1)),
     "ingest_ifds": (1, None),
 }
 

@@ -3,7 +3,7 @@
 the reference's own ioOperation returns on the same files
 (tests/golden/ingest_*.npz, made by tests/golden/make_golden.py from the
 reference's sources compiled for the CPU).  The .wbd scenario
-(tests/wbd.py) has three pitch blocks (45, 15 and 60 pulses), so the
+(tests/wbd.py) has three pitch blocks (45, 15 and 140 pulses), so the
 turn-angle curve's block split, 20-pulse knots, pulse-by-pulse short block,
 absolute-index knot lookup and block offsets are all exercised."""
 import os

@@ -43,11 +43,11 @@ def dropin_dir(root, name):
 
 
 # Ingest scenario shared by the golden generator and the ingest tests: one
-# .wbd file of 120 pulses x 512 range cells whose pitching jumps by more than
+# .wbd file of 200 pulses x 512 range cells whose pitching jumps by more than
 # 0.2 degrees twice, so the turn-angle curve (common.cu:902-972) has three
-# blocks of 45, 15 and 60 pulses (blocks of 21..39 pulses are avoided: the
+# blocks of 45, 15 and 140 pulses (blocks of 21..39 pulses are avoided: the
 # reference's interpolation then reads before its knot vector).
-INGEST_P, INGEST_N = 120, 512
+INGEST_P, INGEST_N = 200, 512
 
 
 def write_ingest_scenario(d, data_type=2, seed=5):
@@ -59,12 +59,12 @@ def write_ingest_scenario(d, data_type=2, seed=5):
     P, N = INGEST_P, INGEST_N
     cfg = dict(M=P, N=N, seed=seed, Fs=128e6, n_scat=30, v0=250.0, accel=-40.0)
     iq, vel = oracle.synth(cfg)
-    pit = np.concatenate([np.full(45, 5.0), np.full(15, 5.5), np.full(60, 6.0)])
+    pit = np.concatenate([np.full(45, 5.0), np.full(15, 5.5), np.full(140, 6.0)])
     # azimuth: slow drift in the long blocks (their knots are 20 pulses
     # apart), 0.1 degree steps in the 15-pulse block, whose curve steps
     # pulse by pulse (smaller steps make the float cosine of the angle round
     # to 1 or above, and the reference's acos then gives 0 or NaN)
-    az = np.concatenate([np.linspace(10.0, 10.2, 45), 10.2 + 0.1 * np.arange(1, 16), 11.7 + 0.01 * np.arange(1, 61)])
+    az = np.concatenate([np.linspace(10.0, 10.2, 45), 10.2 + 0.1 * np.arange(1, 16), 11.7 + 0.01 * np.arange(1, 141)])
     rng = np.linspace(1000.0, 1011.9, P)
     name = "syn_000004_1383_%s_1101.wbd" % ("00" if data_type == 2 else "01")
     path = os.path.join(d, name)
