@@ -603,6 +603,14 @@ ISAR_API int isar_create(isar_ctx** out, const isar_radar* radar, int device, vo
         g_last_error = msg;
         return rc;
     }
+    // Default autofocus engine: the fastest for one frame of M pulses,
+    // measured on a GB300 with the reference's 120 iterations (U = 64..128
+    // selected bins): clusters of 4 / 8 CTAs at 128 / 256 pulses, the
+    // cooperative grid at 512, clusters of 16 at 1024; the cooperative grid
+    // where the device cannot launch that cluster.  Every engine computes
+    // the reference's iteration (the same parity bar).
+    const int pref = M == 128 ? 4 : M == 256 ? 8 : M == 1024 ? 16 : 0;
+    c->af_cluster = (pref > 0 && isar::af_cluster_max(M) >= pref) ? pref : 0;
     *out = c;
     return ISAR_OK;
 }
