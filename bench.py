@@ -332,6 +332,17 @@ def run_gb300(args):
             HI[k].copy_(Id, non_blocking=True)
             d2h_done[k].record(ds)
 
+    # the host->device bandwidth of this machine now (one step's int16 echoes
+    # alone): the end-to-end rate is bounded by it when it falls below the
+    # batch's consumption rate
+    torch.cuda.synchronize()
+    h0, h1 = ev(), ev()
+    h0.record(cs)
+    with torch.cuda.stream(cs):
+        Q[0].copy_(HQ, non_blocking=True)
+    h1.record(cs)
+    cs.synchronize()
+    h2d_alone_ms = h0.elapsed_time(h1)
     for i in range(args.warmup):
         e2e_step(i)
     torch.cuda.synchronize()
@@ -376,7 +387,9 @@ def run_gb300(args):
         "entropy_check": check,
         "e2e": {"value": ws * B / e2e_s, "unit": "frames/s", "h2d_bytes_per_step": B * (M * N * 4 + M * 8),
                 "d2h_bytes_per_step": B * M * C * 4,
-                "input": "int16 I/Q echoes (the sensor format), read directly by range alignment (ISAR_FLAG_IQ16)"},
+                "input": "int16 I/Q echoes (the sensor format), read directly by range alignment (ISAR_FLAG_IQ16)",
+                "ms_per_step": e2e_s * 1e3, "h2d_alone_ms": h2d_alone_ms,
+                "h2d_gbs": B * M * N * 4 / (h2d_alone_ms * 1e-3) / 1e9},
         "roofline": roof,
         "gpu_launches": int(launches),
         "clocks": clk,
