@@ -233,98 +233,88 @@ k_fe_colfft(const float2* __restrict__ cut, const float2* __restrict__ phase, do
     }
 }
 
-// Bin selection (phase_adjustment.cu:248-264), one CTA of 512 threads:
-// stable sort by energy (descending), keep tgt_num, stable sort by entropy
-// (ascending), keep U (indices beyond tgt_num are 0, as device_vector::resize
-// pads), sort the kept indices.  NaN keys sort last.
-__global__ void __launch_bounds__(512)
+// One element per thread of a 512-thread CTA, sorted so that thread i ends
+// with the i-th element in the strict order `before`: strides below 32 are
+// exchanged by warp shuffles, larger ones through shared memory (10 of the
+// 45 stages).  `before` must be a strict order; equal elements are
+// interchangeable (they end in either of their places).
+struct SelKey {
+    double key;
+    int tie;   // tie-break (smaller first)
+    int val;   // payload
+};
+__device__ __forceinline__ SelKey shfl_xor_key(const SelKey& v, int j)
+{
+    SelKey w;
+    w.key = __shfl_xor_sync(0xffffffffu, v.key, j);
+    w.tie = __shfl_xor_sync(0xffffffffu, v.tie, j);
+    w.val = __shfl_xor_sync(0xffffffffu, v.val, j);
+    return w;
+}
+template <class Before>
+__device__ __forceinline__ void sort512(SelKey& v, SelKey* sm, Before before)
+{
+    const int i = threadIdx.x;
+    for (int k = 2; k <= C; k <<= 1)
+        for (int j = k >> 1; j > 0; j >>= 1) {
+            SelKey w;
+            if (j >= 32) {
+                sm[i] = v;
+                __syncthreads();
+                w = sm[i ^ j];
+                __syncthreads();
+            } else {
+                w = shfl_xor_key(v, j);
+            }
+            const bool up = (i & k) == 0;      // this region ascends in `before` order
+            const bool lower = (i & j) == 0;   // i is the lower index of its pair
+            const bool v_first = before(v, w);
+            if (!((lower == up) ? v_first : !v_first)) v = w;
+        }
+}
+
+// Bin selection (phase_adjustment.cu:248-264), one CTA of 512 threads, one
+// column per thread: stable sort by energy (descending), keep tgt_num, stable
+// sort by entropy (ascending), keep U (indices beyond tgt_num are 0, as
+// device_vector::resize pads), sort the kept indices.  NaN keys sort last.
+// The stable sorts are strict orders with the position as tie-break.
+__global__ void __launch_bounds__(C)
 k_fe_select(const double* __restrict__ E, const double* __restrict__ H, int* __restrict__ fdec,
             int* __restrict__ bins)
 {
-    __shared__ double key[C];
-    __shared__ int id[C];
-    __shared__ int pos[C];
+    __shared__ SelKey sm[C];
     const int tid = threadIdx.x;
     const int tgt = fdec[0], U = fdec[1];
+    SelKey v;
     {
-        double e = E[tid];
-        key[tid] = isnan(e) ? -CUDART_INF : e;
-        id[tid] = tid;
+        const double e = E[tid];
+        v.key = isnan(e) ? -CUDART_INF : e;
+        v.tie = tid;
+        v.val = tid;
     }
-    __syncthreads();
-    // bitonic: "a before b" iff key_a > key_b or (== and id_a < id_b)
-    for (int k = 2; k <= C; k <<= 1)
-        for (int j = k >> 1; j > 0; j >>= 1) {
-            const int i = tid, ixj = i ^ j;
-            if (ixj > i) {
-                const bool up = (i & k) == 0;
-                const double ka = key[i], kb = key[ixj];
-                const int ia = id[i], ib = id[ixj];
-                const bool a_first = (ka > kb) || (ka == kb && ia < ib);
-                if (a_first != up) {
-                    key[i] = kb;
-                    key[ixj] = ka;
-                    id[i] = ib;
-                    id[ixj] = ia;
-                }
-            }
-            __syncthreads();
-        }
+    sort512(v, sm, [](const SelKey& a, const SelKey& b) {
+        return a.key > b.key || (a.key == b.key && a.tie < b.tie);
+    });
     // second key: entropy of the first tgt entries; the rest are sentinels
     {
-        const int i = tid;
-        double h = (i < tgt) ? H[id[i]] : CUDART_INF;
+        double h = (tid < tgt) ? H[v.val] : CUDART_INF;
         if (isnan(h)) h = CUDART_INF;
-        const int sel = id[i];
-        __syncthreads();
-        key[i] = h;
-        pos[i] = (i < tgt) ? i : (C + i);
-        id[i] = sel;
+        v.key = h;
+        v.tie = (tid < tgt) ? tid : (C + tid);
     }
-    __syncthreads();
-    for (int k = 2; k <= C; k <<= 1)
-        for (int j = k >> 1; j > 0; j >>= 1) {
-            const int i = tid, ixj = i ^ j;
-            if (ixj > i) {
-                const bool up = (i & k) == 0;
-                const double ka = key[i], kb = key[ixj];
-                const int pa = pos[i], pb = pos[ixj];
-                const bool a_first = (ka < kb) || (ka == kb && pa < pb);
-                if (a_first != up) {
-                    key[i] = kb;
-                    key[ixj] = ka;
-                    pos[i] = pb;
-                    pos[ixj] = pa;
-                    const int t = id[i];
-                    id[i] = id[ixj];
-                    id[ixj] = t;
-                }
-            }
-            __syncthreads();
-        }
+    sort512(v, sm, [](const SelKey& a, const SelKey& b) {
+        return a.key < b.key || (a.key == b.key && a.tie < b.tie);
+    });
     // keep U, pad with 0, sort ascending
     {
-        const int i = tid;
         int b = 0x7fffffff;
-        if (i < U) b = (i < tgt) ? id[i] : 0;
-        __syncthreads();
-        pos[i] = b;
+        if (tid < U) b = (tid < tgt) ? v.val : 0;
+        v.key = 0.0;
+        v.tie = 0;
+        v.val = b;
     }
-    __syncthreads();
-    for (int k = 2; k <= C; k <<= 1)
-        for (int j = k >> 1; j > 0; j >>= 1) {
-            const int i = tid, ixj = i ^ j;
-            if (ixj > i) {
-                const bool up = (i & k) == 0;
-                const int a = pos[i], b = pos[ixj];
-                if ((a > b) == up) {
-                    pos[i] = b;
-                    pos[ixj] = a;
-                }
-            }
-            __syncthreads();
-        }
-    if (tid < U) bins[tid] = pos[tid];
+    sort512(v, sm, [](const SelKey& a, const SelKey& b) { return a.val < b.val; });
+    if (tid < U) bins[tid] = v.val;
 }
 
 // Grid-wide barrier for cooperative launches (all CTAs co-resident): arrive
