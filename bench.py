@@ -337,13 +337,16 @@ def run_gb300(args):
     # alone): the end-to-end rate is bounded by it when it falls below the
     # batch's consumption rate
     torch.cuda.synchronize()
-    h0, h1 = ev(), ev()
-    h0.record(cs)
-    with torch.cuda.stream(cs):
-        Q[0].copy_(HQ, non_blocking=True)
-    h1.record(cs)
-    cs.synchronize()
-    h2d_alone_ms = h0.elapsed_time(h1)
+    h2d_t = []
+    for _ in range(3):   # the first copy also pays one-time mapping costs
+        h0, h1 = ev(), ev()
+        h0.record(cs)
+        with torch.cuda.stream(cs):
+            Q[0].copy_(HQ, non_blocking=True)
+        h1.record(cs)
+        cs.synchronize()
+        h2d_t.append(h0.elapsed_time(h1))
+    h2d_alone_ms = statistics.median(h2d_t)
     for i in range(args.warmup):
         e2e_step(i)
     torch.cuda.synchronize()
