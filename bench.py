@@ -351,11 +351,14 @@ def run_gb300(args):
         e2e_step(i)
     torch.cuda.synchronize()
     barrier(ws)
+    clocks_e2e = Clocks(local)
+    clocks_e2e.start()
     t0 = time.perf_counter()
     for i in range(args.steps):
         e2e_step(i)
     torch.cuda.synchronize()
     e2e_s = max_over_ranks(ws, (time.perf_counter() - t0) / args.steps, dev)
+    clk_e2e = clocks_e2e.stop()
     batch.synchronize()
 
     peak, peak_kind = peaks()
@@ -392,7 +395,7 @@ def run_gb300(args):
         "e2e": {"value": ws * B / e2e_s, "unit": "frames/s", "h2d_bytes_per_step": B * (M * N * 4 + M * 8),
                 "d2h_bytes_per_step": B * M * C * 4,
                 "input": "int16 I/Q echoes (the sensor format), read directly by range alignment (ISAR_FLAG_IQ16)",
-                "ms_per_step": e2e_s * 1e3, "h2d_alone_ms": h2d_alone_ms,
+                "ms_per_step": e2e_s * 1e3, "h2d_alone_ms": h2d_alone_ms, "clocks": clk_e2e,
                 "h2d_gbs": B * M * N * 4 / (h2d_alone_ms * 1e-3) / 1e9},
         "roofline": roof,
         "gpu_launches": int(launches),

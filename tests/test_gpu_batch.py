@@ -60,6 +60,37 @@ def test_batch_equals_single_frame_and_oracle(torch_cuda, gb300):
         assert rel_l2(img, want) < TOL_IMG, (f["M"], f["N"])
 
 
+# the benchmark's frame size and its half, five-stage, beside a plain frame
+LARGE = [(1024, 8192, True, 51), (512, 4096, True, 52), (256, 4096, False, 53), (1024, 8192, True, 54)]
+
+
+def test_batch_of_large_uneven_frames_equals_single_frame_and_oracle(torch_cuda, gb300):
+    torch = torch_cuda
+    fr = []
+    for M, N, full, seed in LARGE:
+        e, v = make_frame(M, N, seed=seed, full=full)
+        fr.append(dict(M=M, N=N, full=full, e=e, v=v, rp=gb300.radar(M, N),
+                       de=torch.from_numpy(np.ascontiguousarray(e, np.complex64).view(np.float32).copy()).cuda(),
+                       dv=torch.from_numpy(np.ascontiguousarray(v, np.float64).copy()).cuda(),
+                       img=torch.full((M, 512), np.nan, dtype=torch.float32, device="cuda"),
+                       flags=(gb300.FLAG_HPC | gb300.FLAG_MTRC) if full else 0))
+    with gb300.Batch(lanes=2) as b:
+        b.run(_batch_list(gb300, fr))
+        b.synchronize()
+        tunings = {(f["M"], f["N"]): b.tuning(f["rp"]) for f in fr}
+    for f in fr:
+        img = f["img"].cpu().numpy()
+        t = tunings[(f["M"], f["N"])]
+        with gb300.Context(f["rp"], stream=torch.cuda.current_stream().cuda_stream) as ctx:
+            ctx.set_tuning(**{k: getattr(t, k) for k in ("ra_rows_each_level", "ra_pair_min", "ra_rows_per_cta",
+                                                         "ra_rows_final", "af_cluster", "af_tol", "af_iters")})
+            single = ctx.image_host(f["e"], f["v"], f["flags"])
+        assert rel_l2(img, single) <= 1e-6, (f["M"], f["N"])
+        want, _ = oracle.image(f["e"], f["v"], oracle.radar(f["M"], f["N"]), hpc=f["full"], mtrc=f["full"])
+        assert rel_l2(img, want) < TOL_IMG, (f["M"], f["N"])
+        assert abs(oracle.entropy(img) - oracle.entropy(want)) < 1e-4
+
+
 def test_batch_autotune_keeps_results(torch_cuda, gb300):
     torch = torch_cuda
     fr = _frames_on_device(torch, gb300)[:4]
@@ -67,7 +98,7 @@ def test_batch_autotune_keeps_results(torch_cuda, gb300):
         lst = _batch_list(gb300, fr)
         ms = b.autotune(lst)
         assert 0.0 < ms < 1e4
-        assert b.lanes() in (1, 2, 4, 8, 16, 32)
+        assert b.lanes() in (1, 2, 4, 8, 16, 32, 64)
         b.run(lst)
         b.synchronize()
         for f in fr:
