@@ -132,6 +132,11 @@ int default_tuning(isar_ctx* c, isar_tuning* t)
     return ISAR_OK;
 }
 
+// Instantiated batch graphs kept per batch (least recently used dropped):
+// enough for a caller that rotates several buffer sets through the same
+// frames (e.g. copy-in / compute / copy-out pipelines) next to a resident set.
+constexpr size_t kBatchGraphs = 8;
+
 int ensure_lanes(isar_batch* b, Shape* s, int n)
 {
     while ((int)s->lanes.size() < n) {
@@ -406,7 +411,7 @@ ISAR_API int isar_batch_run(isar_batch* b, const isar_batch_frame* f, int n)
     BatchGraph g;
     TRY(capture_batch(b, f, n, b->lanes, &g));
     g.tick = b->tick;
-    if (b->graphs.size() >= 4) {
+    if (b->graphs.size() >= kBatchGraphs) {
         auto lru = std::min_element(b->graphs.begin(), b->graphs.end(),
                                     [](const BatchGraph& x, const BatchGraph& y) { return x.tick < y.tick; });
         cudaGraphExecDestroy(lru->exec);
