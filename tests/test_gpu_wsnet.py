@@ -13,15 +13,21 @@ def _bf16_tensor(torch, x):
     return torch.from_numpy(wsnet.bf16(np.asarray(x, np.float32))).cuda().to(torch.bfloat16)
 
 
-@pytest.mark.parametrize("M,N,K,splits", [(256, 64, 320, 1), (300, 16, 64, 1), (320, 64, 4096, 8),
-                                          (128, 320, 64, 1), (200, 16, 1024, 3)])
-def test_gemm_bf16_matches_fp64(torch_cuda, gb300, M, N, K, splits):
+# (rows, columns, K, split-K parts, padding of the operands' leading dimension):
+# the network's inference shape (1024 pulses x 64 channels, K = 320), ragged
+# rows and columns, many K blocks with a partial last one, the weight
+# gradient's shape (K = 65536 pulses in 64 parts), strided operands.
+@pytest.mark.parametrize("M,N,K,splits,pad", [(256, 64, 320, 1, 0), (300, 16, 64, 1, 0), (320, 64, 4096, 8, 0),
+                                              (128, 320, 64, 1, 0), (200, 16, 1024, 3, 0), (1024, 64, 320, 1, 0),
+                                              (1000, 40, 1000, 1, 0), (320, 64, 65536, 64, 0), (130, 24, 328, 2, 24)])
+def test_gemm_bf16_matches_fp64(torch_cuda, gb300, M, N, K, splits, pad):
     torch = torch_cuda
     rng = np.random.default_rng(M + N + K)
-    a = _bf16_tensor(torch, rng.standard_normal((M, K)))
-    b = _bf16_tensor(torch, rng.standard_normal((N, K)))
+    a_full = _bf16_tensor(torch, rng.standard_normal((M, K + pad)))
+    b_full = _bf16_tensor(torch, rng.standard_normal((N, K + pad)))
+    a, b = a_full[:, :K], b_full[:, :K]
     c = torch.full((M, N), np.nan, dtype=torch.float32, device="cuda")
-    gb300.gemm_bf16(a, K, b, K, c, N, M, N, K, splits)
+    gb300.gemm_bf16(a_full, K + pad, b_full, K + pad, c, N, M, N, K, splits)
     torch.cuda.synchronize()
     want = a.double() @ b.double().T
     err = float((c.double() - want).norm() / want.norm())
