@@ -23,10 +23,12 @@ the same way.
 copies its 128 echoes host->device as int16 I/Q samples (the sensor format, 4
 bytes per sample; range alignment reads them directly) and reads the 128
 images back, five buffer sets in rotation so that the copies of the next
-steps overlap the current step's compute (the host->device link of the box
-stalls for ~0.2 s every few gigabytes; five sets give the copies ~0.27 s of
-slack).  Under torchrun every rank images its own frames (replicas, weak
-scaling).
+steps overlap the current step's compute (beside the running batch about one
+host->device copy in seven takes ~0.2 s instead of 20 ms; five sets give the
+copies ~0.27 s of slack), over at least E2E_MIN_STEPS steps so that the
+first step's copy, which starts from idle streams, does not dominate the
+streaming rate.  Under torchrun every rank images its own frames (replicas,
+weak scaling).
 
 --impl reference times the CPU restatement of the reference's chain (the
 oracle) on all host cores, one frame per worker process per step.
@@ -50,6 +52,7 @@ TOL = 3e-7                  # autofocus entropy stop criterion (relative change 
 TOL_LEARNED = 3e-6          # the learned leg's stop criterion (its gain is the same as at 3e-7, 26% fewer iterations)
 E2E_SETS = 5                # end-to-end buffer sets in rotation (copies of later steps run ahead)
 E2E_CHUNKS = 16             # host->device copy of a step in this many pieces
+E2E_MIN_STEPS = 120         # end-to-end steps at least: the streaming rate, not the pipeline's fill
 METRIC = "frames/s @1024×8192 c64: learned+batched vs plain on 1 GB300, equal entropy"
 ARMS = [("learned warm start (to the entropy stop criterion) judged against the plain autofocus (120 iterations) "
          "on final image entropy", True, TOL_LEARNED),
@@ -356,13 +359,20 @@ def run_gb300(args):
         e2e_step(i)
     torch.cuda.synchronize()
     barrier(ws)
+    # The timed loop starts with every stream idle, so its first step waits
+    # for a whole host->device copy, which next to the running batch graph
+    # can take ~0.2 s instead of 20 ms (measured: copies alone never do;
+    # beside the batch about one in seven does, and once the copies run
+    # ahead the buffer sets absorb it).  Enough steps keep that one-time
+    # fill from dominating the streaming rate.
+    e2e_steps = max(args.steps, E2E_MIN_STEPS)
     clocks_e2e = Clocks(local)
     clocks_e2e.start()
     t0 = time.perf_counter()
-    for i in range(args.steps):
+    for i in range(e2e_steps):
         e2e_step(i)
     torch.cuda.synchronize()
-    e2e_s = max_over_ranks(ws, (time.perf_counter() - t0) / args.steps, dev)
+    e2e_s = max_over_ranks(ws, (time.perf_counter() - t0) / e2e_steps, dev)
     clk_e2e = clocks_e2e.stop()
     batch.synchronize()
 
@@ -400,7 +410,7 @@ def run_gb300(args):
         "e2e": {"value": ws * B / e2e_s, "unit": "frames/s", "h2d_bytes_per_step": B * (M * N * 4 + M * 8),
                 "d2h_bytes_per_step": B * M * C * 4,
                 "input": "int16 I/Q echoes (the sensor format), read directly by range alignment (ISAR_FLAG_IQ16)",
-                "ms_per_step": e2e_s * 1e3, "h2d_alone_ms": h2d_alone_ms, "clocks": clk_e2e,
+                "ms_per_step": e2e_s * 1e3, "steps": e2e_steps, "h2d_alone_ms": h2d_alone_ms, "clocks": clk_e2e,
                 "h2d_gbs": B * M * N * 4 / (h2d_alone_ms * 1e-3) / 1e9},
         "roofline": roof,
         "gpu_launches": int(launches),
