@@ -22,10 +22,10 @@ the same way.
 `e2e` goes through the public C ABI with pinned host buffers: every step
 copies its 128 echoes host->device as int16 I/Q samples (the sensor format, 4
 bytes per sample; range alignment reads them directly) and reads the 128
-images back, five buffer sets in rotation so that the copies of the next
+images back, eight buffer sets in rotation so that the copies of the next
 steps overlap the current step's compute (beside the running batch about one
-host->device copy in seven takes ~0.2 s instead of 20 ms; five sets give the
-copies ~0.27 s of slack), over at least E2E_MIN_STEPS steps so that the
+host->device copy in seven takes ~0.2 s instead of 20 ms; eight sets give the
+copies ~0.45 s of slack), over at least E2E_MIN_STEPS steps so that the
 first step's copy, which starts from idle streams, does not dominate the
 streaming rate.  Under torchrun every rank images its own frames (replicas,
 weak scaling).
@@ -50,7 +50,7 @@ C = 512
 B = 128                     # frames per batch step
 TOL = 3e-7                  # autofocus entropy stop criterion (relative change per iteration)
 TOL_LEARNED = 3e-6          # the learned leg's stop criterion (its gain is the same as at 3e-7, 26% fewer iterations)
-E2E_SETS = 5                # end-to-end buffer sets in rotation (copies of later steps run ahead)
+E2E_SETS = 8                # end-to-end buffer sets in rotation (copies of later steps run ahead)
 E2E_CHUNKS = 16             # host->device copy of a step in this many pieces
 E2E_MIN_STEPS = 120         # end-to-end steps at least: the streaming rate, not the pipeline's fill
 METRIC = "frames/s @1024×8192 c64: learned+batched vs plain on 1 GB300, equal entropy"

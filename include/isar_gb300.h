@@ -292,7 +292,7 @@ typedef struct {
 
 typedef struct isar_batch isar_batch;
 
-/* lanes: contexts per frame shape (0 = 4); `stream` = cudaStream_t or NULL. */
+/* lanes: contexts per frame shape, 0..128 (0 = 4); `stream` = cudaStream_t or NULL. */
 ISAR_API int isar_batch_create(isar_batch** out, int device, void* stream, int lanes);
 ISAR_API int isar_batch_destroy(isar_batch* b);
 ISAR_API void* isar_batch_stream(isar_batch* b);
@@ -307,9 +307,10 @@ ISAR_API int isar_batch_lanes(isar_batch* b);
  * and future (isar_set_warmstart); drops cached graphs. */
 ISAR_API int isar_batch_set_warmstart(isar_batch* b, const isar_wsnet* net);
 /* Tunes each shape (isar_autotune, cluster engine), then on the whole frame
- * list the lanes per shape with the cluster size, then the range-alignment
- * envelope path and rows per CTA; *best_ms (may be NULL) = the fastest batch
- * time. */
+ * list the lanes per shape (powers of two up to 128) with the autofocus
+ * cluster size (16, 8 or 4 CTAs), then the range-alignment envelope path and
+ * rows per CTA, by timing whole-batch graph replays; *best_ms (may be NULL)
+ * = the fastest batch time. */
 ISAR_API int isar_batch_autotune(isar_batch* b, const isar_batch_frame* frames, int n, float* best_ms);
 
 /* ---- learned autofocus warm start ----------------------------------------

@@ -135,7 +135,7 @@ int default_tuning(isar_ctx* c, isar_tuning* t)
 // Instantiated batch graphs kept per batch (least recently used dropped):
 // enough for a caller that rotates several buffer sets through the same
 // frames (e.g. copy-in / compute / copy-out pipelines) next to a resident set.
-constexpr size_t kBatchGraphs = 8;
+constexpr size_t kBatchGraphs = 12;
 
 int ensure_lanes(isar_batch* b, Shape* s, int n)
 {
@@ -363,7 +363,7 @@ ISAR_API int isar_autotune(isar_ctx* c, const float* d_echo, const double* d_vel
 ISAR_API int isar_batch_create(isar_batch** out, int device, void* stream, int lanes)
 {
     if (!out) return fail(ISAR_EINVAL, "null output");
-    if (lanes < 0 || lanes > 64) return fail(ISAR_EINVAL, "lanes must be in [0, 64]");
+    if (lanes < 0 || lanes > 128) return fail(ISAR_EINVAL, "lanes must be in [0, 128]");
     std::unique_ptr<isar_batch> b(new isar_batch());
     b->dev = device;
     CU(cudaSetDevice(device));
@@ -475,8 +475,8 @@ ISAR_API int isar_batch_set_warmstart(isar_batch* b, const isar_wsnet* net)
 /*
  * Autotunes `f`: per shape, the launch parameters on the first frame of that
  * shape (isar_autotune with the cluster engine only), then the lanes per
- * shape from {1, 2, 4, 8, 16, 32} (up to the largest frame count of a shape)
- * jointly with the cluster size (16 or 8 CTAs) by timing whole-batch graph
+ * shape from {1, 2, 4, ..., 128} (up to the largest frame count of a shape)
+ * jointly with the cluster size (16, 8 or 4 CTAs) by timing whole-batch graph
  * replays, then on the whole batch again the range-alignment envelope path
  * and rows per CTA (accumulate kernel, then final transform): with many
  * frames in flight fewer, longer CTAs beat the single-frame choice.  The next
@@ -539,9 +539,9 @@ ISAR_API int isar_batch_autotune(isar_batch* b, const isar_batch_frame* f, int n
     };
     float best = 1e30f;
     int best_l = b->lanes, best_cl = 0;
-    for (int cl : {16, 8}) {
+    for (int cl : {16, 8, 4}) {
         TRY(apply(set_cluster(cl)));
-        for (int L : {1, 2, 4, 8, 16, 32, 64}) {
+        for (int L : {1, 2, 4, 8, 16, 32, 64, 128}) {
             if (L > 1 && L / 2 >= most) break;
             float ms = 0.0f;
             TRY(time_with(L, &ms));

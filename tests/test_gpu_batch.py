@@ -98,7 +98,7 @@ def test_batch_autotune_keeps_results(torch_cuda, gb300):
         lst = _batch_list(gb300, fr)
         ms = b.autotune(lst)
         assert 0.0 < ms < 1e4
-        assert b.lanes() in (1, 2, 4, 8, 16, 32, 64)
+        assert b.lanes() in (1, 2, 4, 8, 16, 32, 64, 128)
         b.run(lst)
         b.synchronize()
         for f in fr:
