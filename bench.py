@@ -623,7 +623,7 @@ def run_reference(args):
 def run_profile(args):
     """Profiling workloads (no timing, no JSON): `plain` images one
     1024 x 8192 frame warmup + steps times; `batch` runs a batch of 8 frames
-    through isar_batch_run with the reference algorithm (8-CTA cluster
+    through isar_batch_run with the reference algorithm (4-CTA cluster
     autofocus, 120 iterations); `learned` the same batch with the learned
     warm start and the entropy stop criterion; `ifds` the IFDS pulse
     compression of 1024 pulses of 5000 samples and the HRRP of one
@@ -669,7 +669,9 @@ def run_profile(args):
         with g.Batch(stream=s.cuda_stream, lanes=8) as b:
             if learned:
                 b.set_warmstart(net)
-            b.set_tuning(rp, g.Tuning(ra_pair_min=128, ra_rows_per_cta=16, ra_rows_final=16, af_cluster=8,
+            # the batch's autotuned configuration at 128 frames (one frame per
+            # lane, 4-CTA autofocus clusters, 4 rows per CTA in the final transform)
+            b.set_tuning(rp, g.Tuning(ra_pair_min=128, ra_rows_per_cta=16, ra_rows_final=4, af_cluster=4,
                                       af_tol=TOL_LEARNED if learned else 0.0, af_iters=120, af_cluster_max=0))
             lst = g.Batch.frames((rp, X[i], V[i], flags, imgs[i]) for i in range(nb))
             for _ in range(args.warmup + args.steps):

@@ -29,10 +29,23 @@ __global__ void __launch_bounds__(256) k_mtrc_rows(const float2* __restrict__ cu
 // Bluestein CZT along pulses for CB range bins (mtrc.cu:125-172):
 // y = pre .* x (zero padded to L), Y = FFT_L(y) .* V, y = IFFT_L(Y)/L,
 // out[k] = y[M-1+k] * post[k].
-template <int M, int CB>
+// COLMEAN (M >= 512): the rest of the reference's chain up to the image's
+// magnitude is, per column a of the CZT output, ifftshift / IFFT / M /
+// fftshift (mtrc.cu:53-61), a row FFT (:63-66), the column fftshift (:69),
+// the window on row 0 (isar_main.cu:192; hamming[c / M] = hamming[0] for
+// every column c < 512 when M >= 512) and FFT / fftshift over pulses
+// (isar_main.cu:193-201).  The row FFT commutes with the column operations,
+// and the column operations collapse to a - (1 - hamming[0]) * mean(a):
+// FFT(IFFT(z)/M with element 0 scaled by h) = z + (h - 1) mean(z), and the
+// shifts cancel.  So this kernel writes a - (1 - hamming[0]) mean(a)
+// (flipped up-down for IFDS, isar_main.cu:201-204) and the row transform
+// k_mtrc_rowfft_abs forms the image.  (With M < 512 the window's factor
+// differs between columns and the full chain runs.)
+template <int M, int CB, bool COLMEAN = false>
 __global__ void __launch_bounds__(CB * (2 * M) / 16)
 k_czt(const float2* __restrict__ st, const float2* __restrict__ pre, const float2* __restrict__ post,
-      const float2* __restrict__ V, float2* __restrict__ out, const float2* __restrict__ tw)
+      const float2* __restrict__ V, float2* __restrict__ out, const float2* __restrict__ tw,
+      const float* __restrict__ hamM = nullptr, int flipud = 0)
 {
     constexpr int L = 2 * M;
     using F = FFTShape<L>;
@@ -61,10 +74,49 @@ k_czt(const float2* __restrict__ st, const float2* __restrict__ pre, const float
                       },
                       sm, lt, tw);
     __syncthreads();
-    for (int i = tid; i < M * CB; i += blockDim.x) {
-        const int k = i / CB, cc = i % CB;
-        const size_t g = (size_t)k * C + c0 + cc;
-        out[g] = cmul(tile[i], post[g]);
+    if constexpr (!COLMEAN) {
+        for (int i = tid; i < M * CB; i += blockDim.x) {
+            const int k = i / CB, cc = i % CB;
+            const size_t g = (size_t)k * C + c0 + cc;
+            out[g] = cmul(tile[i], post[g]);
+        }
+    } else {
+        static_assert((CB * (2 * M) / 16) % CB == 0 && CB <= 32, "a thread keeps one column");
+        __shared__ double2 red[CB * (2 * M) / 16 / 32][CB];
+        __shared__ float2 sub[CB];
+        // a = y * post in place; this thread's column is tid % CB
+        double sx = 0.0, sy = 0.0;
+        for (int i = tid; i < M * CB; i += blockDim.x) {
+            const int k = i / CB, cc = i % CB;
+            const float2 v = cmul(tile[i], post[(size_t)k * C + c0 + cc]);
+            tile[i] = v;
+            sx += v.x;
+            sy += v.y;
+        }
+#pragma unroll
+        for (int o = 16; o >= CB; o >>= 1) {
+            sx += __shfl_xor_sync(0xffffffffu, sx, o);
+            sy += __shfl_xor_sync(0xffffffffu, sy, o);
+        }
+        const int lane = tid & 31, w = tid >> 5;
+        if (lane < CB) red[w][lane] = make_double2(sx, sy);
+        __syncthreads();
+        if (tid < CB) {
+            double ax = 0.0, ay = 0.0;
+            for (int q = 0; q < (int)(blockDim.x >> 5); ++q) {
+                ax += red[q][tid].x;
+                ay += red[q][tid].y;
+            }
+            const double f = (1.0 - (double)__ldg(&hamM[0])) / (double)M;
+            sub[tid] = make_float2((float)(ax * f), (float)(ay * f));
+        }
+        __syncthreads();
+        for (int i = tid; i < M * CB; i += blockDim.x) {
+            const int k = i / CB, cc = i % CB;
+            const int r = flipud ? M - 1 - k : k;
+            const float2 v = tile[i], d = sub[cc];
+            out[(size_t)r * C + c0 + cc] = make_float2(v.x - d.x, v.y - d.y);
+        }
     }
 }
 
@@ -111,6 +163,26 @@ __global__ void __launch_bounds__(256) k_mtrc_rowfft(const float2* __restrict__ 
                            int d = (i + C / 2) & (C - 1);
                            if (fliplr) d = C - 1 - d;
                            o[d] = v;
+                       },
+                       smb + team * F::SMEM, lt, tw);
+}
+
+// The image from the column-corrected MTRC rows (see k_czt, COLMEAN):
+// |fftshift(FFT(row))| per row, IFDS flipped left-right (mtrc.cu:63-75).
+__global__ void __launch_bounds__(256) k_mtrc_rowfft_abs(const float2* __restrict__ in, float* __restrict__ img,
+                                                         int fliplr, const float2* __restrict__ tw)
+{
+    using F = FFTShape<C>;
+    __shared__ float2 smb[8 * F::SMEM];
+    const int team = threadIdx.x / F::T, lt = threadIdx.x % F::T;
+    const int m = blockIdx.x * 8 + team;
+    const float2* xr = in + (size_t)m * C;
+    float* o = img + (size_t)m * C;
+    team_fft<C, false>([&](int i) { return xr[i]; },
+                       [&](int i, float2 v, int) {
+                           int d = (i + C / 2) & (C - 1);
+                           if (fliplr) d = C - 1 - d;
+                           o[d] = sqrtf(v.x * v.x + v.y * v.y);
                        },
                        smb + team * F::SMEM, lt, tw);
 }
@@ -178,6 +250,10 @@ static cudaError_t post_run_m(const PostArgs& a, cudaStream_t st)
             return -(int)e;
         if ((e = cudaFuncSetAttribute(k_czt<M, CZ>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_czt)))
             return -(int)e;
+        if constexpr (M >= 512)
+            if ((e = cudaFuncSetAttribute(k_czt<M, CZ, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                          (int)smem_czt)))
+                return -(int)e;
         return 0;
     });
     if (ar < 0) return (cudaError_t)(-ar);
@@ -187,6 +263,16 @@ static cudaError_t post_run_m(const PostArgs& a, cudaStream_t st)
         if (a.data_type == 1) k_mtrc_rows<false><<<M / 8, 256, 0, st>>>(a.cut, a.st, a.tw);
         else k_mtrc_rows<true><<<M / 8, 256, 0, st>>>(a.cut, a.st, a.tw);
         ISAR_COUNT(1);
+        if constexpr (M >= 512) {
+            // the column IFFT, window and column FFT as one column correction
+            // (see k_czt, COLMEAN), then the rows form the image
+            k_czt<M, CZ, true><<<C / CZ, CZ * FL::T, smem_czt, st>>>(a.st, a.pre, a.post, a.V, a.st2, a.tw,
+                                                                      a.hamM, a.data_type == 1);
+            ISAR_COUNT(1);
+            k_mtrc_rowfft_abs<<<M / 8, 256, 0, st>>>(a.st2, a.img, a.data_type == 1, a.tw);
+            ISAR_COUNT(1);
+            return cudaGetLastError();
+        }
         k_czt<M, CZ><<<C / CZ, CZ * FL::T, smem_czt, st>>>(a.st, a.pre, a.post, a.V, a.st2, a.tw);
         ISAR_COUNT(1);
         k_mtrc_cols<M, CB><<<C / CB, CB * F::T, smem_cols, st>>>(a.st2, a.st, a.tw);

@@ -141,15 +141,20 @@ def test_fast_entropy_stage(torch_cuda, gb300, M, N, seed, af_cluster):
     assert rel_l2(out, out_want) < TOL_IMG
 
 
-@pytest.mark.parametrize("M,mtrc", [(128, False), (256, True), (1024, True)])
-def test_post_stage(torch_cuda, gb300, M, mtrc):
+# MTRC at M >= 512 forms the image through the column correction of k_czt
+# (the column IFFT, window and column FFT collapsed), M < 512 through the
+# reference's full chain; IFDS adds both flips.
+@pytest.mark.parametrize("M,mtrc,ifds", [(128, False, False), (256, True, False), (512, True, False),
+                                         (1024, True, False), (1024, True, True), (256, True, True)])
+def test_post_stage(torch_cuda, gb300, M, mtrc, ifds):
     torch = torch_cuda
     N = 1024 if M < 1024 else 2048
     rng = np.random.default_rng(M)
     cut = (rng.standard_normal((M, 512)) + 1j * rng.standard_normal((M, 512))).astype(np.complex64)
     rp = oracle.radar(M, N)
-    want = oracle.post(oracle.mtrc(cut, rp) if mtrc else cut)
-    with ctx_for(gb300, torch, M, N) as ctx:
+    dt = oracle.IFDS if ifds else oracle.STRETCH
+    want = oracle.post(oracle.mtrc(cut, rp, dt) if mtrc else cut, dt)
+    with ctx_for(gb300, torch, M, N, data_type=gb300.IFDS if ifds else gb300.STRETCH) as ctx:
         dc = to_dev(torch, cut)
         img = torch.empty((M, 512), dtype=torch.float32, device="cuda")
         ctx.stage_post(dc, img, gb300.FLAG_MTRC if mtrc else 0)
