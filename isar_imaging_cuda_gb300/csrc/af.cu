@@ -1225,6 +1225,7 @@ static cudaError_t fe_run_m(const FEArgs& a, cudaStream_t st)
             return e;
         ISAR_COUNT(1);
     }
+    if (a.defer_apply) return cudaGetLastError();   // the imaging applies the phase(s)
     if (a.ws_w && a.iters > 0 && a.af_cluster > 0)
         k_af_apply2<<<M, 256, 0, st>>>(a.cut, a.phase, a.ws_phase, a.cut2, M);
     else

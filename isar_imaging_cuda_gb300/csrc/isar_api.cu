@@ -460,12 +460,25 @@ int run_frame_eager(isar_ctx* c, const float2* x, const double* d_vel, int flags
     }
     TRY(run_range_align(c, x, c->d_x, d_vel, flags));
     CU(isar::center_cut(c->d_arp, c->d_x, c->M, c->N, c->d_dec, c->d_cut, c->st));
-    CU(isar::fe_run(fe_args(c, c->d_cut, c->af_iters), c->st));
-    CU(isar::post_run(post_args(c, c->d_cut, flags, d_img), c->st));
+    // With MTRC at 512 pulses or more the imaging applies the autofocus
+    // phase itself (in the CZT's load), so the cut stays unphased and the
+    // rows' transform of the MTRC is shared by both legs of a warm start.
+    const bool fold = (flags & ISAR_FLAG_MTRC) && c->M >= 512;
+    isar::FEArgs fa = fe_args(c, c->d_cut, c->af_iters);
+    fa.defer_apply = fold ? 1 : 0;
+    CU(isar::fe_run(fa, c->st));
+    isar::PostArgs pa = post_args(c, c->d_cut, flags, d_img);
+    if (fold) pa.phase = c->d_phase;
+    CU(isar::post_run(pa, c->st));
     if (c->ws_w && c->af_iters > 0) {
         // warm start: image the learned leg too; the judge keeps the lower
         // final image entropy in d_img
-        CU(isar::post_run(post_args(c, c->d_cut2, flags, c->d_img2), c->st));
+        isar::PostArgs pl = post_args(c, fold ? c->d_cut : c->d_cut2, flags, c->d_img2);
+        if (fold) {
+            pl.phase = c->d_ws_phase;
+            pl.rows_ready = 1;
+        }
+        CU(isar::post_run(pl, c->st));
         CU(isar::img_judge(d_img, c->d_img2, c->M * kRangeCut, c->d_judge, c->d_fdec + 4, c->st));
     }
     return ISAR_OK;

@@ -129,6 +129,8 @@ struct FEArgs {
     float2* cut2;            // [M][512] the learned leg's phase applied to the cut (warm start)
     int* ws_err;             // GEMM wait-timeout flag
     int pre_only;            // stop after the bin selection and the Doppler start phase
+    int defer_apply;         // leave the cut unphased: the imaging applies the phase(s)
+                             // (PostArgs::phase; MTRC at M >= 512 only)
 };
 
 // Largest cluster the device accepts for the autofocus engine with M pulses
@@ -157,6 +159,12 @@ struct PostArgs {
     const float* hamM;       // [M]
     float* img;              // [M][512]
     const float2* tw;
+    // MTRC at M >= 512 only: the per-pulse phase the imaging applies to the
+    // cut (the CZT's load; a row transform commutes with a per-row factor),
+    // or nullptr when the cut is already phased; rows_ready: st already
+    // holds the rows' transform of this cut (the second leg of a frame).
+    const float2* phase;
+    int rows_ready;
 };
 
 cudaError_t hpc_coef(const double* vel, int M, double coef_over_fs2, int64_t* hq, cudaStream_t st);

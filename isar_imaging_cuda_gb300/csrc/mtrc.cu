@@ -41,11 +41,13 @@ __global__ void __launch_bounds__(256) k_mtrc_rows(const float2* __restrict__ cu
 // (flipped up-down for IFDS, isar_main.cu:201-204) and the row transform
 // k_mtrc_rowfft_abs forms the image.  (With M < 512 the window's factor
 // differs between columns and the full chain runs.)
+// phase (may be null): the autofocus phase of pulse k, applied here instead
+// of to the cut (the rows' transform before this kernel is linear per row).
 template <int M, int CB, bool COLMEAN = false>
 __global__ void __launch_bounds__(CB * (2 * M) / 16)
 k_czt(const float2* __restrict__ st, const float2* __restrict__ pre, const float2* __restrict__ post,
       const float2* __restrict__ V, float2* __restrict__ out, const float2* __restrict__ tw,
-      const float* __restrict__ hamM = nullptr, int flipud = 0)
+      const float* __restrict__ hamM = nullptr, int flipud = 0, const float2* __restrict__ phase = nullptr)
 {
     constexpr int L = 2 * M;
     using F = FFTShape<L>;
@@ -58,7 +60,8 @@ k_czt(const float2* __restrict__ st, const float2* __restrict__ pre, const float
     for (int i = tid; i < M * CB; i += blockDim.x) {
         const int k = i / CB, cc = i % CB;
         const size_t g = (size_t)k * C + c0 + cc;
-        tile[i] = cmul(pre[g], st[g]);
+        const float2 v = cmul(pre[g], st[g]);
+        tile[i] = phase ? cmul(v, phase[k]) : v;
     }
     __syncthreads();
     float2* sm = smb + team * F::SMEM;
@@ -259,15 +262,19 @@ static cudaError_t post_run_m(const PostArgs& a, cudaStream_t st)
     if (ar < 0) return (cudaError_t)(-ar);
     int src_shift = 0;
     const float2* src = a.cut;
+    if ((a.phase || a.rows_ready) && !(a.mtrc && M >= 512)) return cudaErrorInvalidValue;
     if (a.mtrc) {
-        if (a.data_type == 1) k_mtrc_rows<false><<<M / 8, 256, 0, st>>>(a.cut, a.st, a.tw);
-        else k_mtrc_rows<true><<<M / 8, 256, 0, st>>>(a.cut, a.st, a.tw);
-        ISAR_COUNT(1);
+        if (!a.rows_ready) {
+            if (a.data_type == 1) k_mtrc_rows<false><<<M / 8, 256, 0, st>>>(a.cut, a.st, a.tw);
+            else k_mtrc_rows<true><<<M / 8, 256, 0, st>>>(a.cut, a.st, a.tw);
+            ISAR_COUNT(1);
+        }
         if constexpr (M >= 512) {
             // the column IFFT, window and column FFT as one column correction
-            // (see k_czt, COLMEAN), then the rows form the image
+            // (see k_czt, COLMEAN), then the rows form the image; st is only
+            // read from here on, so a second leg reuses it (rows_ready)
             k_czt<M, CZ, true><<<C / CZ, CZ * FL::T, smem_czt, st>>>(a.st, a.pre, a.post, a.V, a.st2, a.tw,
-                                                                      a.hamM, a.data_type == 1);
+                                                                      a.hamM, a.data_type == 1, a.phase);
             ISAR_COUNT(1);
             k_mtrc_rowfft_abs<<<M / 8, 256, 0, st>>>(a.st2, a.img, a.data_type == 1, a.tw);
             ISAR_COUNT(1);
