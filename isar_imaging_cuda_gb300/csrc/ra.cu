@@ -908,7 +908,9 @@ k_ra_final(const float2* x, float2* yout, const float* __restrict__ win, const i
 __global__ void k_arp_reduce(const float* __restrict__ part, int nparts, int N, int M,
                              const unsigned* __restrict__ hmax, float* __restrict__ arp)
 {
-    const float inv = 1.0f / __uint_as_float(*hmax);
+    // an all-zero frame (max 0) gives a zero profile rather than 0/0
+    const float hm = __uint_as_float(*hmax);
+    const float inv = hm > 0.0f ? 1.0f / hm : 0.0f;
     const float invM = 1.0f / (float)M;
     for (int n = blockIdx.x * blockDim.x + threadIdx.x; n < N; n += gridDim.x * blockDim.x) {
         float s = 0.0f;
@@ -979,6 +981,95 @@ __device__ __forceinline__ T block_sum_1024(T v, T* red)
     return v;
 }
 
+// Ascending sort of the n non-negative floats in s (their bit patterns order
+// as unsigned integers), one CTA of 1024 threads: an LSD radix sort, four
+// passes of 8-bit digits.  Threads t < n / 8 (whole warps, n >= 256) hold 8
+// keys each; slot e of lane l of warp w is element 256 w + 32 e + l of the
+// current order, which every pass keeps stable: within a warp a key's rank
+// among equal digits comes from __match_any_sync and a running count per
+// (digit, warp) over the slots, across warps from an exclusive scan of the
+// counts in digit-major order.  cnt: 256 * (n / 256 + 1) ints (one pad
+// column against bank conflicts); red: 32 ints.
+__device__ void block_radix_sort(float* s, int n, int* cnt, int* red)
+{
+    const int T = n / 8, W = T / 32, WP = W + 1;
+    const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
+    const bool act = tid < T;
+    const unsigned lt_mask = (1u << lane) - 1u;
+    unsigned k[8];
+    int off[8];
+#pragma unroll 1
+    for (int shift = 0; shift < 32; shift += 8) {
+        for (int i = tid; i < 256 * WP; i += blockDim.x) cnt[i] = 0;
+        if (act) {
+#pragma unroll
+            for (int e = 0; e < 8; ++e) k[e] = __float_as_uint(s[256 * w + 32 * e + lane]);
+        }
+        __syncthreads();   // keys loaded, counters cleared
+        if (act) {
+#pragma unroll
+            for (int e = 0; e < 8; ++e) {
+                const int d = (int)((k[e] >> shift) & 255u);
+                const unsigned peers = __match_any_sync(0xffffffffu, d);
+                const int rank = __popc(peers & lt_mask);
+                const int base = cnt[d * WP + w];
+                off[e] = base + rank;
+                __syncwarp();
+                if (rank == 0) cnt[d * WP + w] = base + __popc(peers);
+                __syncwarp();
+            }
+        }
+        __syncthreads();
+        // exclusive scan of cnt over f = d * W + w: q consecutive entries per
+        // thread, then the threads' totals across the block
+        const int total = 256 * W;
+        const int q = (total + (int)blockDim.x - 1) / (int)blockDim.x;   // <= 8
+        const int f0 = tid * q;
+        int loc[8];
+        int sum = 0;
+#pragma unroll
+        for (int j = 0; j < 8; ++j) {
+            loc[j] = sum;
+            const int f = f0 + j;
+            if (j < q && f < total) sum += cnt[(f / W) * WP + f % W];
+        }
+        int x = sum;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const int y = __shfl_up_sync(0xffffffffu, x, o);
+            if (lane >= o) x += y;
+        }
+        if (lane == 31) red[w] = x;
+        __syncthreads();
+        if (w == 0) {
+            const int v = lane < (int)(blockDim.x >> 5) ? red[lane] : 0;
+            int z = v;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const int y = __shfl_up_sync(0xffffffffu, z, o);
+                if (lane >= o) z += y;
+            }
+            red[lane] = z - v;
+        }
+        __syncthreads();
+        const int excl = red[w] + x - sum;
+#pragma unroll
+        for (int j = 0; j < 8; ++j) {
+            const int f = f0 + j;
+            if (j < q && f < total) cnt[(f / W) * WP + f % W] = excl + loc[j];
+        }
+        __syncthreads();   // cnt holds each (digit, warp) start
+        if (act) {
+#pragma unroll
+            for (int e = 0; e < 8; ++e) {
+                const int d = (int)((k[e] >> shift) & 255u);
+                s[cnt[d * WP + w] + off[e]] = __uint_as_float(k[e]);
+            }
+        }
+        __syncthreads();
+    }
+}
+
 // HRRPCenter decisions + cutRangeProfile offset, one CTA of 1024 threads.
 // dec: [0] applied, [1] shift_num, [2] cut offset, [3] |idx_1|, [4] |idx_2|,
 //      [5] threshold (float bits).
@@ -993,6 +1084,7 @@ k_center(const float* __restrict__ arp_g, const float2* __restrict__ y, int N, i
     __shared__ int red_i[32];
     __shared__ float red_f[32];
     __shared__ int red_j[32];
+    __shared__ int sort_cnt[256 * (kMaxN / 256 + 1)];
     const int tid = threadIdx.x;
     for (int i = tid; i < N; i += blockDim.x) {
         const float v = arp_g[i];
@@ -1000,76 +1092,9 @@ k_center(const float* __restrict__ arp_g, const float2* __restrict__ y, int N, i
         srt[i] = v;
     }
     __syncthreads();
-    // bitonic sort ascending (thrust::stable_sort of arp1, :404; values only,
-    // so stability does not show).  Threads t < N/8 hold elements 8t..8t+7 in
-    // registers: strides below 8 are swaps in registers, strides 8..255
-    // shuffles within a warp, and only strides of 256 and more go through
-    // shared memory (15 of the 91 stages at N = 8192).
-    {
-        const int T = N / 8;
-        const bool act = tid < T;
-        float v[8];
-        if (act) {
-#pragma unroll
-            for (int e = 0; e < 8; ++e) v[e] = srt[8 * tid + e];
-        }
-        __syncthreads();
-        for (int k = 2; k <= N; k <<= 1) {
-            for (int jj = k >> 1; jj > 0; jj >>= 1) {
-                if (jj >= 256) {
-                    if (act) {
-#pragma unroll
-                        for (int e = 0; e < 8; ++e) srt[8 * tid + e] = v[e];
-                    }
-                    __syncthreads();
-                    if (act) {
-                        const int p = tid ^ (jj >> 3);
-                        const bool low = (tid & (jj >> 3)) == 0;   // element i < its partner
-#pragma unroll
-                        for (int e = 0; e < 8; ++e) {
-                            const float w = srt[8 * p + e];
-                            const bool up = ((8 * tid + e) & k) == 0;
-                            v[e] = (low == up) ? fminf(v[e], w) : fmaxf(v[e], w);
-                        }
-                    }
-                    __syncthreads();
-                } else if (jj >= 8) {
-                    if (act) {
-                        const int o = jj >> 3;
-                        const bool low = (tid & o) == 0;
-#pragma unroll
-                        for (int e = 0; e < 8; ++e) {
-                            const float w = __shfl_xor_sync(0xffffffffu, v[e], o);
-                            const bool up = ((8 * tid + e) & k) == 0;
-                            v[e] = (low == up) ? fminf(v[e], w) : fmaxf(v[e], w);
-                        }
-                    }
-                } else if (act) {
-                    // in registers; the stride as a constant keeps v[] in registers
-                    auto swaps = [&](auto J) {
-                        constexpr int jc = decltype(J)::value;
-#pragma unroll
-                        for (int e = 0; e < 8; ++e) {
-                            if ((e & jc) == 0) {
-                                const bool up = ((8 * tid + e) & k) == 0;
-                                const float a = v[e], b = v[e | jc];
-                                v[e] = up ? fminf(a, b) : fmaxf(a, b);
-                                v[e | jc] = up ? fmaxf(a, b) : fminf(a, b);
-                            }
-                        }
-                    };
-                    if (jj == 4) swaps(std::integral_constant<int, 4>{});
-                    else if (jj == 2) swaps(std::integral_constant<int, 2>{});
-                    else swaps(std::integral_constant<int, 1>{});
-                }
-            }
-        }
-        if (act) {
-#pragma unroll
-            for (int e = 0; e < 8; ++e) srt[8 * tid + e] = v[e];
-        }
-        __syncthreads();
-    }
+    // ascending sort (thrust::stable_sort of arp1, :404; values only, so
+    // stability does not show)
+    block_radix_sort(srt, N, sort_cnt, red_i);
     // extra = inter_length * max(arp1) / N ; diff argmin (first index) (:406-420)
     const float arp1_max = srt[N - 1];
     const float extra = (float)inter_length * arp1_max / (float)N;
@@ -1108,7 +1133,8 @@ k_center(const float* __restrict__ arp_g, const float2* __restrict__ y, int N, i
         red_j[0] = ii;
     }
     __syncthreads();
-    const int dmin = red_j[0];
+    // a profile without a finite minimum (NaN everywhere) keeps index 0
+    const int dmin = red_j[0] < dl ? red_j[0] : 0;
     __syncthreads();
     const float thr = srt[dmin + inter_length / 2];
     // idx_1 = find(arp > thr); drop those whose 9-tap mean < thr (:426-449)
