@@ -993,6 +993,7 @@ __device__ __forceinline__ T block_sum_1024(T v, T* red)
 __device__ void block_radix_sort(float* s, int n, int* cnt, int* red)
 {
     const int T = n / 8, W = T / 32, WP = W + 1;
+    const int lw = 31 - __clz(W);   // W = n / 256 is a power of two
     const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
     const bool act = tid < T;
     const unsigned lt_mask = (1u << lane) - 1u;
@@ -1031,7 +1032,7 @@ __device__ void block_radix_sort(float* s, int n, int* cnt, int* red)
         for (int j = 0; j < 8; ++j) {
             loc[j] = sum;
             const int f = f0 + j;
-            if (j < q && f < total) sum += cnt[(f / W) * WP + f % W];
+            if (j < q && f < total) sum += cnt[(f >> lw) * WP + (f & (W - 1))];
         }
         int x = sum;
 #pragma unroll
@@ -1056,7 +1057,7 @@ __device__ void block_radix_sort(float* s, int n, int* cnt, int* red)
 #pragma unroll
         for (int j = 0; j < 8; ++j) {
             const int f = f0 + j;
-            if (j < q && f < total) cnt[(f / W) * WP + f % W] = excl + loc[j];
+            if (j < q && f < total) cnt[(f >> lw) * WP + (f & (W - 1))] = excl + loc[j];
         }
         __syncthreads();   // cnt holds each (digit, warp) start
         if (act) {
