@@ -99,7 +99,8 @@ def test_range_align_stage(torch_cuda, gb300, M, N, hpc, rows_each_level):
     assert rel_l2(y2, y_want) < TOL_IMG
 
 
-@pytest.mark.parametrize("M,N", [(128, 1024), (256, 4096)])
+# N = 512 and 8192 are the two ends of the centring sort (2 and 32 warps).
+@pytest.mark.parametrize("M,N", [(128, 512), (128, 1024), (256, 4096), (512, 8192)])
 def test_center_cut_stage(torch_cuda, gb300, M, N):
     torch = torch_cuda
     e, _ = make_frame(M, N, seed=7 * M + N)
