@@ -126,7 +126,8 @@ struct FEArgs {
     nn::Acts* ws_a;          // inference activations for M rows; act[0] receives the features
     float* ws_psi;           // [M]
     float2* ws_phase;        // [M] warm-start phase in, the learned leg's final phase out
-    float2* cut2;            // [M][512] the learned leg's phase applied to the cut (warm start)
+    float2* cut2;            // [M][512] the learned leg's phase applied to the cut (warm start;
+                             // not written with defer_apply, where the imaging applies it)
     int* ws_err;             // GEMM wait-timeout flag
     int pre_only;            // stop after the bin selection and the Doppler start phase
     int defer_apply;         // leave the cut unphased: the imaging applies the phase(s)
