@@ -795,7 +795,6 @@ ISAR_API int isar_set_warmstart(isar_ctx* c, const isar_wsnet* net)
         c->ws_a.rows = c->M;
         for (int l = 0; l < isar::nn::kConv + 2; ++l) TRY(dalloc(c, &c->ws_a.act[l], M * isar::nn::kCh));
         TRY(dalloc(c, &c->ws_a.col, M * isar::nn::kColK));
-        TRY(dalloc(c, &c->ws_a.z, M * isar::nn::kCh));
         TRY(dalloc(c, &c->ws_a.out, M * isar::nn::kOutPad));
         TRY(dalloc(c, &c->d_ws_psi, M));
         TRY(dalloc(c, &c->d_ws_phase, M));

@@ -52,26 +52,6 @@ __global__ void k_im2col(const __nv_bfloat16* __restrict__ act, int frames, int 
     }
 }
 
-// out[p][c] = bf16(relu(z[p][c] + bias[c])), c < 64.
-__global__ void k_bias_relu(const float* __restrict__ z, const float* __restrict__ bias, long rows,
-                            __nv_bfloat16* __restrict__ out)
-{
-    const long n = rows * kCh;
-    for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) {
-        const float v = z[i] + bias[i & (kCh - 1)];
-        out[i] = __float2bfloat16_rn(v > 0.0f ? v : 0.0f);
-    }
-}
-
-// out[p][0..1] += bias[0..1].
-__global__ void k_bias_out(float* __restrict__ out, const float* __restrict__ bias, long rows)
-{
-    for (long p = blockIdx.x * (long)blockDim.x + threadIdx.x; p < rows; p += (long)gridDim.x * blockDim.x) {
-        out[p * kOutPad + 0] += bias[0];
-        out[p * kOutPad + 1] += bias[1];
-    }
-}
-
 // Per frame: delta_m = atan2(s, c) - r_m (m < M-1), z = mean exp(j delta),
 // loss = 1 - |z|; d loss / d r_hat_m = Im(conj(z) exp(j delta_m)) / ((M-1) |z|)
 // / frames, chained through r_hat = atan2(s, c) into dout (bf16 [rows][16]).
@@ -380,22 +360,31 @@ cudaError_t forward(const Weights& w, Acts& a, int frames, int M, int* err, cuda
     const long rows = (long)frames * M;
     if (rows > a.rows) return cudaErrorInvalidValue;
     cudaError_t e;
+    // every hidden layer: bias and ReLU in the GEMM's epilogue, bf16 out
+    auto hidden = [&](int l) {
+        GemmEpilogue ep;
+        ep.bias = w.master + b_off(l);
+        ep.out_bf16 = a.act[l + 1];
+        ep.ld_bf16 = kCh;
+        return ep;
+    };
     for (int l = 0; l < kConv; ++l) {
         __nv_bfloat16* col = a.cols[l] ? a.cols[l] : a.col;
         k_im2col<<<grid_for(rows * kTaps * (kCh / 8), 256), 256, 0, st>>>(a.act[l], frames, M, col);
         ISAR_COUNT(1);
-        if ((e = gemm_tn(col, kColK, w.w[l], kColK, a.z, kCh, (int)rows, kCh, kColK, 1, err, st))) return e;
-        k_bias_relu<<<grid_for(rows * kCh, 256), 256, 0, st>>>(a.z, w.master + b_off(l), rows, a.act[l + 1]);
-        ISAR_COUNT(1);
+        if ((e = gemm_tn(col, kColK, w.w[l], kColK, nullptr, kCh, (int)rows, kCh, kColK, 1, err, st, hidden(l))))
+            return e;
     }
-    if ((e = gemm_tn(a.act[kConv], kCh, w.w[kConv], kCh, a.z, kCh, (int)rows, kCh, kCh, 1, err, st))) return e;
-    k_bias_relu<<<grid_for(rows * kCh, 256), 256, 0, st>>>(a.z, w.master + b_off(kConv), rows, a.act[kConv + 1]);
-    ISAR_COUNT(1);
-    if ((e = gemm_tn(a.act[kConv + 1], kCh, w.w[kConv + 1], kCh, a.out, kOutPad, (int)rows, kOutPad, kCh, 1, err,
-                     st)))
+    if ((e = gemm_tn(a.act[kConv], kCh, w.w[kConv], kCh, nullptr, kCh, (int)rows, kCh, kCh, 1, err, st,
+                     hidden(kConv))))
         return e;
-    k_bias_out<<<grid_for(rows, 256), 256, 0, st>>>(a.out, w.master + b_off(kConv + 1), rows);
-    ISAR_COUNT(1);
+    // output layer: bias on the two used columns (c, s)
+    GemmEpilogue eo;
+    eo.bias = w.master + b_off(kConv + 1);
+    eo.bias_cols = 2;
+    if ((e = gemm_tn(a.act[kConv + 1], kCh, w.w[kConv + 1], kCh, a.out, kOutPad, (int)rows, kOutPad, kCh, 1, err,
+                     st, eo)))
+        return e;
     return cudaGetLastError();
 }
 

@@ -48,12 +48,22 @@ struct Acts {
     __nv_bfloat16* act[kConv + 2] = {};       // act[0] = X0 (caller-filled), act[l+1] = layer l output [rows][64]
     __nv_bfloat16* col = nullptr;             // [rows][320] im2col scratch (inference) or
     __nv_bfloat16* cols[kConv] = {};          // per conv layer (training keeps them for the weight gradients)
-    float* z = nullptr;                       // [rows][320] fp32 GEMM output scratch
     float* out = nullptr;                     // [rows][16] network output (c, s, 14 pad)
 };
 
+// Optional epilogue of gemm_tn (no split-K): with out_bf16, the tile is
+// written as bf16(max(C + bias[c], 0)) to out_bf16 [Mr][ld_bf16] (16-byte
+// aligned rows) instead of C; otherwise, with bias, columns c < bias_cols of
+// C get bias[c] added.
+struct GemmEpilogue {
+    const float* bias = nullptr;
+    __nv_bfloat16* out_bf16 = nullptr;
+    int ld_bf16 = 0;
+    int bias_cols = 0;
+};
+
 cudaError_t gemm_tn(const __nv_bfloat16* A, int lda, const __nv_bfloat16* B, int ldb, float* C, int ldc, int Mr,
-                    int Nc, int K, int splits, int* err, cudaStream_t st);
+                    int Nc, int K, int splits, int* err, cudaStream_t st, const GemmEpilogue& ep = GemmEpilogue{});
 
 // Refreshes the bf16 copies (and transposes) from the fp32 master.
 cudaError_t refresh_bf16(const Weights& w, cudaStream_t st);

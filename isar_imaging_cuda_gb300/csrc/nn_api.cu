@@ -122,7 +122,6 @@ ISAR_API int isar_wsnet_create(isar_wsnet** out, int max_rows, int training, int
     n->a.rows = max_rows;
     for (int l = 1; l < kConv + 2; ++l)
         if ((rc = nalloc(n.get(), &n->a.act[l], R * kCh)) != ISAR_OK) return fin(rc);
-    if ((rc = nalloc(n.get(), &n->a.z, R * kCh)) != ISAR_OK) return fin(rc);
     if ((rc = nalloc(n.get(), &n->a.out, R * kOutPad)) != ISAR_OK) return fin(rc);
     if (n->training) {
         for (int l = 0; l < kConv; ++l)

@@ -25,6 +25,7 @@
 #include <stdint.h>
 
 #include "isar_kernels.h"
+#include "nn.h"
 
 namespace isar {
 namespace nn {
@@ -112,7 +113,8 @@ __device__ __forceinline__ void umma_commit(uint32_t bar)
 template <int BN>
 __global__ void __launch_bounds__(128, 1)
 k_gemm_tn(const __grid_constant__ CUtensorMap map_a, const __grid_constant__ CUtensorMap map_b,
-          float* __restrict__ Cm, int ldc, int Mr, int Nc, int K, int klen, int atomic_out, int* err)
+          float* __restrict__ Cm, int ldc, int Mr, int Nc, int K, int klen, int atomic_out, int* err,
+          const float* __restrict__ bias, __nv_bfloat16* __restrict__ out_bf16, int ld_bf16, int bias_cols)
 {
     static_assert(BN == 16 || BN == 32 || BN == 64, "tile N");
     using S = GemmSmem<BN>;
@@ -233,12 +235,38 @@ k_gemm_tn(const __grid_constant__ CUtensorMap map_a, const __grid_constant__ CUt
                 : "r"(taddr)
                 : "memory");
             asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
-            if (r < Mr) {
+            if (r < Mr && out_bf16) {
+                // bf16(max(C + bias, 0)): a hidden layer's activation
+                const int cb = col0 + c0;
+                if (cb + 16 <= Nc) {
+                    uint32_t pk[8];
+#pragma unroll
+                    for (int j = 0; j < 8; ++j) {
+                        const float a0 = __uint_as_float(v[2 * j]) + __ldg(&bias[cb + 2 * j]);
+                        const float a1 = __uint_as_float(v[2 * j + 1]) + __ldg(&bias[cb + 2 * j + 1]);
+                        const __nv_bfloat162 h = __floats2bfloat162_rn(a0 > 0.0f ? a0 : 0.0f, a1 > 0.0f ? a1 : 0.0f);
+                        pk[j] = *reinterpret_cast<const uint32_t*>(&h);
+                    }
+                    uint4* dst = reinterpret_cast<uint4*>(out_bf16 + (size_t)r * ld_bf16 + cb);
+                    dst[0] = make_uint4(pk[0], pk[1], pk[2], pk[3]);
+                    dst[1] = make_uint4(pk[4], pk[5], pk[6], pk[7]);
+                } else {
+#pragma unroll
+                    for (int j = 0; j < 16; ++j) {
+                        const int c = cb + j;
+                        if (c < Nc) {
+                            const float a = __uint_as_float(v[j]) + __ldg(&bias[c]);
+                            out_bf16[(size_t)r * ld_bf16 + c] = __float2bfloat16_rn(a > 0.0f ? a : 0.0f);
+                        }
+                    }
+                }
+            } else if (r < Mr) {
 #pragma unroll
                 for (int j = 0; j < 16; ++j) {
                     const int c = col0 + c0 + j;
                     if (c < Nc) {
-                        const float x = __uint_as_float(v[j]);
+                        float x = __uint_as_float(v[j]);
+                        if (c < bias_cols) x += __ldg(&bias[c]);
                         if (atomic_out) atomicAdd(&Cm[(size_t)r * ldc + c], x);
                         else Cm[(size_t)r * ldc + c] = x;
                     }
@@ -287,7 +315,8 @@ static cudaError_t operand_map(CUtensorMap* m, const __nv_bfloat16* p, int rows,
 
 template <int BN>
 static cudaError_t launch_gemm(const CUtensorMap& ma, const CUtensorMap& mb, dim3 grid, float* C, int ldc, int Mr,
-                               int Nc, int K, int klen, int atomic_out, int* err, cudaStream_t st)
+                               int Nc, int K, int klen, int atomic_out, int* err, cudaStream_t st,
+                               const GemmEpilogue& ep)
 {
     static PerDevice attr;   // the stage ring's dynamic shared-memory limit, once per device
     const int a = attr.get([] {
@@ -297,16 +326,24 @@ static cudaError_t launch_gemm(const CUtensorMap& ma, const CUtensorMap& mb, dim
                    : -1;
     });
     if (a < 0) return cudaErrorInvalidConfiguration;
-    k_gemm_tn<BN><<<grid, 128, GemmSmem<BN>::kBytes, st>>>(ma, mb, C, ldc, Mr, Nc, K, klen, atomic_out, err);
+    k_gemm_tn<BN><<<grid, 128, GemmSmem<BN>::kBytes, st>>>(ma, mb, C, ldc, Mr, Nc, K, klen, atomic_out, err, ep.bias,
+                                                          ep.out_bf16, ep.ld_bf16, ep.bias ? ep.bias_cols : 0);
     return cudaSuccess;
 }
 
 cudaError_t gemm_tn(const __nv_bfloat16* A, int lda, const __nv_bfloat16* B, int ldb, float* C, int ldc, int Mr,
-                    int Nc, int K, int splits, int* err, cudaStream_t st)
+                    int Nc, int K, int splits, int* err, cudaStream_t st, const GemmEpilogue& ep)
 {
     if (Mr <= 0 || Nc <= 0 || K <= 0 || (K % 8) || (lda % 8) || (ldb % 8) || lda < K || ldb < K || splits < 1)
         return cudaErrorInvalidValue;
     if ((reinterpret_cast<uintptr_t>(A) | reinterpret_cast<uintptr_t>(B)) & 15) return cudaErrorMisalignedAddress;
+    // the epilogues need whole sums (no split-K); the bf16 output is stored
+    // 16 bytes at a time, C is not written
+    if ((ep.out_bf16 || ep.bias) && splits != 1) return cudaErrorInvalidValue;
+    if (ep.out_bf16 && (!ep.bias || ep.ld_bf16 < Nc || (ep.ld_bf16 % 8) ||
+                        (reinterpret_cast<uintptr_t>(ep.out_bf16) & 15)))
+        return cudaErrorInvalidValue;
+    if (!ep.out_bf16 && !C) return cudaErrorInvalidValue;
     // split boundaries are multiples of BK, so every copy starts at a K
     // offset of a multiple of 128 bytes and no block crosses into the next
     // split's range (only the last split's last block reaches past K: zeros)
@@ -321,9 +358,9 @@ cudaError_t gemm_tn(const __nv_bfloat16* A, int lda, const __nv_bfloat16* B, int
     if ((e = operand_map(&mb, B, Nc, K, ldb, bn))) return e;
     dim3 grid((Mr + BM - 1) / BM, (Nc + bn - 1) / bn, kz);
     switch (bn) {
-    case 16: e = launch_gemm<16>(ma, mb, grid, C, ldc, Mr, Nc, K, klen, atomic_out, err, st); break;
-    case 32: e = launch_gemm<32>(ma, mb, grid, C, ldc, Mr, Nc, K, klen, atomic_out, err, st); break;
-    default: e = launch_gemm<64>(ma, mb, grid, C, ldc, Mr, Nc, K, klen, atomic_out, err, st); break;
+    case 16: e = launch_gemm<16>(ma, mb, grid, C, ldc, Mr, Nc, K, klen, atomic_out, err, st, ep); break;
+    case 32: e = launch_gemm<32>(ma, mb, grid, C, ldc, Mr, Nc, K, klen, atomic_out, err, st, ep); break;
+    default: e = launch_gemm<64>(ma, mb, grid, C, ldc, Mr, Nc, K, klen, atomic_out, err, st, ep); break;
     }
     if (e) return e;
     ISAR_COUNT(1);
