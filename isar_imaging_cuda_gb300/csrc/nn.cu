@@ -369,6 +369,20 @@ cudaError_t forward(const Weights& w, Acts& a, int frames, int M, int* err, cuda
         return ep;
     };
     for (int l = 0; l < kConv; ++l) {
+        if (!a.cols[l] && M % 128 == 0) {
+            // inference: the conv's im2col operand read tap by tap from the
+            // activations by the GEMM itself (training keeps the columns for
+            // the weight gradients)
+            GemmConvA cv;
+            cv.act = a.act[l];
+            cv.frames = frames;
+            cv.M = M;
+            cv.pad = kTaps / 2;
+            if ((e = gemm_tn(nullptr, kColK, w.w[l], kColK, nullptr, kCh, (int)rows, kCh, kColK, 1, err, st,
+                             hidden(l), cv)))
+                return e;
+            continue;
+        }
         __nv_bfloat16* col = a.cols[l] ? a.cols[l] : a.col;
         k_im2col<<<grid_for(rows * kTaps * (kCh / 8), 256), 256, 0, st>>>(a.act[l], frames, M, col);
         ISAR_COUNT(1);

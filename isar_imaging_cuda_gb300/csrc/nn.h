@@ -62,8 +62,20 @@ struct GemmEpilogue {
     int bias_cols = 0;
 };
 
+// Optional implicit-convolution A operand of gemm_tn: with act set, A is the
+// im2col matrix of act ([frames][M][64] bf16, M a multiple of 128), i.e.
+// A[b*M + m][k*64 + c] = act[b][m + k - pad][c] (0 outside the frame), read
+// tap by tap straight from act; A and lda are ignored and K = taps * 64.
+struct GemmConvA {
+    const __nv_bfloat16* act = nullptr;
+    int frames = 0;
+    int M = 0;
+    int pad = 0;
+};
+
 cudaError_t gemm_tn(const __nv_bfloat16* A, int lda, const __nv_bfloat16* B, int ldb, float* C, int ldc, int Mr,
-                    int Nc, int K, int splits, int* err, cudaStream_t st, const GemmEpilogue& ep = GemmEpilogue{});
+                    int Nc, int K, int splits, int* err, cudaStream_t st, const GemmEpilogue& ep = GemmEpilogue{},
+                    const GemmConvA& conv = GemmConvA{});
 
 // Refreshes the bf16 copies (and transposes) from the fp32 master.
 cudaError_t refresh_bf16(const Weights& w, cudaStream_t st);

@@ -104,6 +104,17 @@ __device__ __forceinline__ void tma_load_2d(uint32_t dst, const CUtensorMap* map
         : "memory");
 }
 
+// Tiled 3-D copy of the box at (x, y, z); y may lie partly outside the
+// tensor (rows there read as zero).
+__device__ __forceinline__ void tma_load_3d(uint32_t dst, const CUtensorMap* map, int x, int y, int z, uint32_t bar)
+{
+    asm volatile(
+        "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], "
+        "[%5];\n" ::"r"(dst),
+        "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(z), "r"(bar)
+        : "memory");
+}
+
 __device__ __forceinline__ void umma_commit(uint32_t bar)
 {
     asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(bar)
@@ -114,7 +125,8 @@ template <int BN>
 __global__ void __launch_bounds__(128, 1)
 k_gemm_tn(const __grid_constant__ CUtensorMap map_a, const __grid_constant__ CUtensorMap map_b,
           float* __restrict__ Cm, int ldc, int Mr, int Nc, int K, int klen, int atomic_out, int* err,
-          const float* __restrict__ bias, __nv_bfloat16* __restrict__ out_bf16, int ld_bf16, int bias_cols)
+          const float* __restrict__ bias, __nv_bfloat16* __restrict__ out_bf16, int ld_bf16, int bias_cols,
+          int conv_M, int conv_pad)
 {
     static_assert(BN == 16 || BN == 32 || BN == 64, "tile N");
     using S = GemmSmem<BN>;
@@ -161,7 +173,15 @@ k_gemm_tn(const __grid_constant__ CUtensorMap map_a, const __grid_constant__ CUt
             const uint32_t fb = smem_u32(&full[s]);
             const uint32_t sa = base + (uint32_t)(s * S::kStage);
             mbar_expect_tx(fb, (uint32_t)S::kStage);
-            tma_load_2d(sa, &map_a, k_beg + b * BK, row0, fb);
+            if (conv_M) {
+                // implicit convolution: K block = tap, rows shifted by
+                // tap - pad within the frame of this row block
+                const int f = row0 / conv_M, m0 = row0 - f * conv_M;
+                const int tap = k_beg / BK + b;
+                tma_load_3d(sa, &map_a, 0, m0 + tap - conv_pad, f, fb);
+            } else {
+                tma_load_2d(sa, &map_a, k_beg + b * BK, row0, fb);
+            }
             tma_load_2d(sa + S::kA, &map_b, k_beg + b * BK, col0, fb);
         };
         const int pre = min(kStages - 1, nblk);
@@ -313,10 +333,27 @@ static cudaError_t operand_map(CUtensorMap* m, const __nv_bfloat16* p, int rows,
     return r == CUDA_SUCCESS ? cudaSuccess : cudaErrorInvalidValue;
 }
 
+// Tensor map of act [frames][M][64] bf16 in boxes of 64 x 128 x 1 with the
+// 128-byte swizzle (the implicit convolution's A operand).
+static cudaError_t conv_map(CUtensorMap* m, const __nv_bfloat16* act, int frames, int M)
+{
+    const PFN_cuTensorMapEncodeTiled_v12000 fn = encode_tiled();
+    if (!fn) return cudaErrorNotSupported;
+    const cuuint64_t dims[3] = {(cuuint64_t)BK, (cuuint64_t)M, (cuuint64_t)frames};
+    const cuuint64_t strides[2] = {(cuuint64_t)BK * sizeof(__nv_bfloat16),
+                                   (cuuint64_t)M * BK * sizeof(__nv_bfloat16)};
+    const cuuint32_t box[3] = {(cuuint32_t)BK, (cuuint32_t)BM, 1};
+    const cuuint32_t estr[3] = {1, 1, 1};
+    const CUresult r = fn(m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 3, const_cast<__nv_bfloat16*>(act), dims, strides, box,
+                          estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+                          CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    return r == CUDA_SUCCESS ? cudaSuccess : cudaErrorInvalidValue;
+}
+
 template <int BN>
 static cudaError_t launch_gemm(const CUtensorMap& ma, const CUtensorMap& mb, dim3 grid, float* C, int ldc, int Mr,
                                int Nc, int K, int klen, int atomic_out, int* err, cudaStream_t st,
-                               const GemmEpilogue& ep)
+                               const GemmEpilogue& ep, const GemmConvA& conv)
 {
     static PerDevice attr;   // the stage ring's dynamic shared-memory limit, once per device
     const int a = attr.get([] {
@@ -327,13 +364,23 @@ static cudaError_t launch_gemm(const CUtensorMap& ma, const CUtensorMap& mb, dim
     });
     if (a < 0) return cudaErrorInvalidConfiguration;
     k_gemm_tn<BN><<<grid, 128, GemmSmem<BN>::kBytes, st>>>(ma, mb, C, ldc, Mr, Nc, K, klen, atomic_out, err, ep.bias,
-                                                          ep.out_bf16, ep.ld_bf16, ep.bias ? ep.bias_cols : 0);
+                                                          ep.out_bf16, ep.ld_bf16, ep.bias ? ep.bias_cols : 0,
+                                                          conv.act ? conv.M : 0, conv.pad);
     return cudaSuccess;
 }
 
 cudaError_t gemm_tn(const __nv_bfloat16* A, int lda, const __nv_bfloat16* B, int ldb, float* C, int ldc, int Mr,
-                    int Nc, int K, int splits, int* err, cudaStream_t st, const GemmEpilogue& ep)
+                    int Nc, int K, int splits, int* err, cudaStream_t st, const GemmEpilogue& ep,
+                    const GemmConvA& conv)
 {
+    if (conv.act) {
+        // row blocks stay inside one frame; the taps are whole K blocks
+        if (conv.M <= 0 || (conv.M % BM) || conv.frames <= 0 || (long)conv.frames * conv.M != Mr || (K % BK) ||
+            conv.pad < 0 || splits != 1 || (reinterpret_cast<uintptr_t>(conv.act) & 15))
+            return cudaErrorInvalidValue;
+        A = conv.act;   // alignment checks below; the map is 3-D
+        lda = K;
+    }
     if (Mr <= 0 || Nc <= 0 || K <= 0 || (K % 8) || (lda % 8) || (ldb % 8) || lda < K || ldb < K || splits < 1)
         return cudaErrorInvalidValue;
     if ((reinterpret_cast<uintptr_t>(A) | reinterpret_cast<uintptr_t>(B)) & 15) return cudaErrorMisalignedAddress;
@@ -354,13 +401,17 @@ cudaError_t gemm_tn(const __nv_bfloat16* A, int lda, const __nv_bfloat16* B, int
     const int bn = Nc <= 16 ? 16 : Nc <= 32 ? 32 : 64;
     CUtensorMap ma, mb;
     cudaError_t e;
-    if ((e = operand_map(&ma, A, Mr, K, lda, BM))) return e;
+    if (conv.act) {
+        if ((e = conv_map(&ma, conv.act, conv.frames, conv.M))) return e;
+    } else if ((e = operand_map(&ma, A, Mr, K, lda, BM))) {
+        return e;
+    }
     if ((e = operand_map(&mb, B, Nc, K, ldb, bn))) return e;
     dim3 grid((Mr + BM - 1) / BM, (Nc + bn - 1) / bn, kz);
     switch (bn) {
-    case 16: e = launch_gemm<16>(ma, mb, grid, C, ldc, Mr, Nc, K, klen, atomic_out, err, st, ep); break;
-    case 32: e = launch_gemm<32>(ma, mb, grid, C, ldc, Mr, Nc, K, klen, atomic_out, err, st, ep); break;
-    default: e = launch_gemm<64>(ma, mb, grid, C, ldc, Mr, Nc, K, klen, atomic_out, err, st, ep); break;
+    case 16: e = launch_gemm<16>(ma, mb, grid, C, ldc, Mr, Nc, K, klen, atomic_out, err, st, ep, conv); break;
+    case 32: e = launch_gemm<32>(ma, mb, grid, C, ldc, Mr, Nc, K, klen, atomic_out, err, st, ep, conv); break;
+    default: e = launch_gemm<64>(ma, mb, grid, C, ldc, Mr, Nc, K, klen, atomic_out, err, st, ep, conv); break;
     }
     if (e) return e;
     ISAR_COUNT(1);
